@@ -1,0 +1,818 @@
+// dd_api.cu -- host side of the C ABI (include/dedisp_gb300.h).
+//
+// Geometry and delay tables are computed on the host in the reference's float
+// expression order (src/Shifts.cpp:20-42); plans turn an observation, a mode
+// and the host tables (shifts, zapped mask, beam mapping) into the group and
+// entry descriptors the kernels read (dd_internal.h), pick a compiled tile
+// configuration, and launch it on the caller's stream.  There is no CPU path.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cctype>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/dedisp_gb300.h"
+#include "dd_internal.h"
+
+namespace {
+
+thread_local std::string g_error;
+
+dd_status fail(dd_status code, const char *fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_error = buf;
+  return code;
+}
+
+dd_status cuda_fail(cudaError_t e, const char *what) {
+  (void)cudaGetLastError();
+  if (e == cudaErrorMemoryAllocation)
+    return fail(DD_ERR_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+    return fail(DD_ERR_NO_DEVICE, "%s: %s", what, cudaGetErrorString(e));
+  return fail(DD_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define DD_CUDA(call, what)                       \
+  do {                                            \
+    cudaError_t e_ = (call);                      \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+bool bits_ok(uint32_t bits) {
+  return bits == 1 || bits == 2 || bits == 4 || bits == 8 || bits == 16 ||
+         bits == 32;
+}
+
+uint64_t pad(uint64_t v, uint64_t p) { return p == 0 ? v : (v + p - 1) / p * p; }
+
+// AstroData::Observation frequency getters.  The subband frequency is that
+// of the subband's highest channel, the channel step one dedisperses each
+// subband to (include/Dedispersion.hpp:124).
+float max_freq(const dd_observation *o) {
+  volatile float span = (o->nr_channels - 1) * o->channel_bandwidth;
+  return o->min_freq + span;
+}
+float subband_bandwidth(const dd_observation *o) {
+  return (o->nr_channels / o->nr_subbands) * o->channel_bandwidth;
+}
+float subband_min_freq(const dd_observation *o) {
+  volatile float span = ((o->nr_channels / o->nr_subbands) - 1) * o->channel_bandwidth;
+  return o->min_freq + span;
+}
+float subband_max_freq(const dd_observation *o) {
+  volatile float span = (o->nr_subbands - 1) * subband_bandwidth(o);
+  return subband_min_freq(o) + span;
+}
+
+// src/Shifts.cpp:20-42, one table: frequencies f0 + k * step for k < n - 1,
+// reference frequency fmax, last entry 0.
+void shift_table(const dd_observation *o, float f0, float step, float fmax,
+                 uint32_t n, float *out) {
+  float inverseHighFreq = 1.0f / std::pow(fmax, 2.0f);
+  float timeUnit = o->nr_samples_per_batch * o->sampling_time;
+  for (uint32_t k = 0; k + 1 < n; k++) {
+    volatile float offset = k * step;
+    float inverseFreq = 1.0f / std::pow(f0 + offset, 2.0f);
+    volatile float a = 4148.808f * (inverseFreq - inverseHighFreq);
+    volatile float b = a * (o->nr_samples_per_batch / o->downsampling);
+    out[k] = b / timeUnit;
+  }
+  out[n - 1] = 0;
+}
+
+uint64_t row_bytes_of(uint32_t samples, uint32_t bits, uint32_t padding) {
+  if (bits < 8) {
+    uint32_t per = 8 / bits;
+    return pad((samples + per - 1) / per, padding);
+  }
+  uint32_t eb = bits / 8;
+  return pad(samples, padding / eb) * eb;
+}
+
+dd_status check_obs(const dd_observation *o, dd_mode mode) {
+  if (!o) return fail(DD_ERR_INVALID_ARGUMENT, "observation is NULL");
+  if (o->downsampling != 1)
+    return fail(DD_ERR_UNSUPPORTED, "downsampling must be 1 (got %u)", o->downsampling);
+  if (o->nr_channels == 0) return fail(DD_ERR_INVALID_ARGUMENT, "nr_channels is 0");
+  if (mode != DD_SINGLE_STEP && (o->nr_subbands == 0 || o->nr_subbands > o->nr_channels))
+    return fail(DD_ERR_INVALID_ARGUMENT, "nr_subbands must be in 1..nr_channels");
+  if (!(o->first_dm >= 0.0f) || !(o->dm_step >= 0.0f) ||
+      !(o->first_dm_subbanding >= 0.0f) || !(o->dm_step_subbanding >= 0.0f))
+    return fail(DD_ERR_INVALID_ARGUMENT, "DM first/step must be non-negative");
+  if (mode < DD_SINGLE_STEP || mode > DD_STEP_TWO)
+    return fail(DD_ERR_INVALID_ARGUMENT, "unknown mode %d", (int)mode);
+  return DD_OK;
+}
+
+// Per-mode dimensions.
+struct Dims {
+  uint32_t nr_dms, nr_samples, row_samples;
+  float first_dm, dm_step;
+  uint64_t row_bytes, out_row, input_bytes, output_rows;
+  uint64_t mapping_row, zapped_elems, shift_elems;
+};
+
+Dims dims_of(const dd_observation *o, dd_mode mode, uint32_t bits, uint32_t padding) {
+  Dims d{};
+  const uint64_t C = o->nr_channels;
+  if (mode == DD_SINGLE_STEP) {
+    d.nr_dms = o->nr_dms; d.nr_samples = o->nr_samples_per_batch;
+    d.row_samples = o->nr_samples_per_dispersed_batch;
+    d.first_dm = o->first_dm; d.dm_step = o->dm_step;
+    d.row_bytes = row_bytes_of(d.row_samples, bits, padding);
+    d.out_row = pad(d.nr_samples, padding / 4);
+    d.input_bytes = o->nr_beams * C * d.row_bytes;
+    d.output_rows = (uint64_t)o->nr_synthesized_beams * o->nr_dms;
+    d.mapping_row = pad(C, padding / 4);
+    d.zapped_elems = pad(C, padding / 4);
+    d.shift_elems = pad(C, padding / 4);
+  } else if (mode == DD_STEP_ONE) {
+    d.nr_dms = o->nr_dms_subbanding; d.nr_samples = o->nr_samples_per_batch_subbanding;
+    d.row_samples = o->nr_samples_per_dispersed_batch_subbanding;
+    d.first_dm = o->first_dm_subbanding; d.dm_step = o->dm_step_subbanding;
+    d.row_bytes = row_bytes_of(d.row_samples, bits, padding);
+    d.out_row = pad(d.nr_samples, padding / 4);
+    d.input_bytes = o->nr_beams * C * d.row_bytes;
+    d.output_rows = (uint64_t)o->nr_beams * o->nr_dms_subbanding * o->nr_subbands;
+    d.mapping_row = 0;
+    d.zapped_elems = pad(C, padding / 4);
+    d.shift_elems = pad(C, padding / 4);
+  } else {
+    d.nr_dms = o->nr_dms; d.nr_samples = o->nr_samples_per_batch;
+    d.row_samples = o->nr_samples_per_batch_subbanding;
+    d.first_dm = o->first_dm; d.dm_step = o->dm_step;
+    d.row_bytes = pad(d.row_samples, padding / 4) * 4;
+    d.out_row = pad(d.nr_samples, padding / 4);
+    d.input_bytes = (uint64_t)o->nr_beams * o->nr_dms_subbanding * o->nr_subbands * d.row_bytes;
+    d.output_rows = (uint64_t)o->nr_synthesized_beams * o->nr_dms_subbanding * o->nr_dms;
+    d.mapping_row = pad(o->nr_subbands, padding / 4);
+    d.zapped_elems = 0;
+    d.shift_elems = pad(o->nr_subbands, padding / 4);
+  }
+  return d;
+}
+
+uint32_t family_bits(dd_mode mode, uint32_t bits) {
+  if (mode == DD_STEP_TWO) return 32;
+  return bits <= 8 ? 8 : bits;
+}
+
+const dd::KernelInfo *find_kernel(dd_mode mode, uint32_t bits, const dd_conf &c) {
+  int n = 0;
+  const dd::KernelInfo *reg = dd::kernel_registry(&n);
+  const uint32_t fb = family_bits(mode, bits);
+  for (int i = 0; i < n; i++) {
+    const dd::KernelInfo &k = reg[i];
+    if ((uint32_t)k.elem_bits != fb) continue;
+    if (c.threads_d0 != 32u || c.threads_d1 != (uint32_t)k.warps_d) continue;
+    if (c.items_d0 != (uint32_t)k.items_t || c.items_d1 != (uint32_t)k.items_d) continue;
+    if (c.unroll != (uint32_t)k.channels) continue;
+    return &k;
+  }
+  return nullptr;
+}
+
+dd_conf conf_of(const dd::KernelInfo &k) {
+  dd_conf c{};
+  c.split_batches = 0; c.local_mem = 1; c.unroll = k.channels;
+  c.threads_d0 = 32; c.threads_d1 = k.warps_d; c.threads_d2 = 1;
+  c.items_d0 = k.items_t; c.items_d1 = k.items_d; c.items_d2 = 1;
+  return c;
+}
+
+dd_status device_ok() {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    (void)cudaGetLastError();
+    return fail(DD_ERR_NO_DEVICE, "no CUDA device available (%s)",
+                e == cudaSuccess ? "0 devices" : cudaGetErrorString(e));
+  }
+  return DD_OK;
+}
+
+// Restores the caller's current device on scope exit.
+struct DeviceGuard {
+  int prev = -1;
+  bool ok = false;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) { (void)cudaGetLastError(); prev = -1; }
+    ok = cudaSetDevice(dev) == cudaSuccess;
+    if (!ok) (void)cudaGetLastError();
+  }
+  ~DeviceGuard() { if (prev >= 0) cudaSetDevice(prev); }
+};
+
+}  // namespace
+
+struct dd_plan {
+  int device = 0;
+  dd_observation obs{};
+  dd_mode mode = DD_SINGLE_STEP;
+  uint32_t bits = 8, padding = 0;
+  const dd::KernelInfo *kinfo = nullptr;
+  Dims dims{};
+  std::vector<float> shifts;
+  std::vector<uint32_t> zapped, mapping;
+  bool have_shifts = false;
+  // derived
+  uint32_t nr_groups = 0, tiles_t = 0, tiles_d = 0, win = 0;
+  size_t smem = 0;
+  uint64_t out_dm_stride = 0;
+  std::vector<dd::GroupDesc> groups;
+  std::vector<dd::EntryDesc> entries;
+  dd::GroupDesc *d_groups = nullptr;
+  dd::EntryDesc *d_entries = nullptr;
+  size_t cap_groups = 0, cap_entries = 0;
+  uint32_t *d_status = nullptr;
+  bool ready = false;
+};
+
+namespace {
+
+// Build the group/entry tables, the window size and upload them.
+dd_status rebuild(dd_plan *p) {
+  p->ready = false;
+  if (!p->have_shifts) return DD_OK;
+  const dd_observation *o = &p->obs;
+  const Dims &d = p->dims;
+  const uint32_t C = o->nr_channels;
+  p->groups.clear();
+  p->entries.clear();
+  auto zapped = [&](uint32_t c) { return !p->zapped.empty() && p->zapped[c] != 0; };
+  if (p->mode == DD_SINGLE_STEP) {
+    p->nr_groups = o->nr_synthesized_beams;
+    p->out_dm_stride = d.out_row;
+    for (uint32_t g = 0; g < p->nr_groups; g++) {
+      dd::GroupDesc G{(uint32_t)p->entries.size(), 0, (uint64_t)g * d.nr_dms * d.out_row};
+      for (uint32_t c = 0; c < C; c++) {
+        if (zapped(c)) continue;
+        uint64_t beam = p->mapping.empty() ? (o->nr_beams ? g % o->nr_beams : 0)
+                                           : p->mapping[(uint64_t)g * d.mapping_row + c];
+        if (beam >= o->nr_beams)
+          return fail(DD_ERR_INVALID_ARGUMENT, "beam mapping[%u][%u] = %llu >= nr_beams %u",
+                      g, c, (unsigned long long)beam, o->nr_beams);
+        p->entries.push_back({(beam * C + c) * d.row_bytes, p->shifts[c], 0});
+      }
+      G.entry_count = (uint32_t)p->entries.size() - G.entry_begin;
+      p->groups.push_back(G);
+    }
+  } else if (p->mode == DD_STEP_ONE) {
+    const uint32_t SB = o->nr_subbands, cps = C / SB;
+    p->nr_groups = o->nr_beams * SB;
+    p->out_dm_stride = (uint64_t)SB * d.out_row;
+    for (uint32_t b = 0; b < o->nr_beams; b++)
+      for (uint32_t sb = 0; sb < SB; sb++) {
+        dd::GroupDesc G{(uint32_t)p->entries.size(), 0,
+                        ((uint64_t)b * d.nr_dms * SB + sb) * d.out_row};
+        const float last = p->shifts[(sb + 1) * cps - 1];
+        for (uint32_t c = sb * cps; c < (sb + 1) * cps; c++) {
+          if (zapped(c)) continue;
+          volatile float rel = p->shifts[c] - last;
+          p->entries.push_back({((uint64_t)b * C + c) * d.row_bytes, rel, 0});
+        }
+        G.entry_count = (uint32_t)p->entries.size() - G.entry_begin;
+        p->groups.push_back(G);
+      }
+  } else {
+    const uint32_t SB = o->nr_subbands, D1 = o->nr_dms_subbanding;
+    p->nr_groups = o->nr_synthesized_beams * D1;
+    p->out_dm_stride = d.out_row;
+    for (uint32_t g = 0; g < o->nr_synthesized_beams; g++)
+      for (uint32_t d1 = 0; d1 < D1; d1++) {
+        dd::GroupDesc G{(uint32_t)p->entries.size(), SB,
+                        ((uint64_t)g * D1 * d.nr_dms + (uint64_t)d1 * d.nr_dms) * d.out_row};
+        for (uint32_t s = 0; s < SB; s++) {
+          uint64_t beam = p->mapping.empty() ? (o->nr_beams ? g % o->nr_beams : 0)
+                                             : p->mapping[(uint64_t)g * d.mapping_row + s];
+          if (beam >= o->nr_beams)
+            return fail(DD_ERR_INVALID_ARGUMENT, "beam mapping[%u][%u] = %llu >= nr_beams %u",
+                        g, s, (unsigned long long)beam, o->nr_beams);
+          p->entries.push_back({((beam * D1 + d1) * SB + s) * d.row_bytes, p->shifts[s], 0});
+        }
+        p->groups.push_back(G);
+      }
+  }
+  // Largest delay must stay inside the rows; window spread per DM tile.
+  const dd::KernelInfo &k = *p->kinfo;
+  std::vector<float> uniq;
+  uniq.reserve(p->entries.size());
+  for (auto &e : p->entries) uniq.push_back(e.shift);
+  std::sort(uniq.begin(), uniq.end());
+  uniq.erase(std::unique(uniq.begin(), uniq.end()), uniq.end());
+  uint32_t max_delay = 0, spread = 0;
+  p->tiles_d = d.nr_dms ? (d.nr_dms + k.tile_d - 1) / k.tile_d : 0;
+  p->tiles_t = d.nr_samples ? (d.nr_samples + k.tile_t - 1) / k.tile_t : 0;
+  for (float sh : uniq) {
+    if (!(sh >= 0.0f) || !std::isfinite(sh))
+      return fail(DD_ERR_INVALID_ARGUMENT, "delay per unit DM must be finite and >= 0 (got %g)", sh);
+    if (d.nr_dms == 0) break;
+    max_delay = std::max(max_delay, dd::host_delay(d.first_dm, d.dm_step, d.nr_dms - 1, sh));
+    for (uint32_t t = 0; t < p->tiles_d; t++) {
+      uint32_t d0 = t * k.tile_d, d1 = std::min(d0 + k.tile_d, d.nr_dms) - 1;
+      uint32_t sp = dd::host_delay(d.first_dm, d.dm_step, d1, sh) -
+                    dd::host_delay(d.first_dm, d.dm_step, d0, sh);
+      spread = std::max(spread, sp);
+    }
+  }
+  if (d.nr_dms && d.nr_samples && (uint64_t)d.nr_samples + max_delay > d.row_samples)
+    return fail(DD_ERR_INVALID_ARGUMENT,
+                "rows hold %u samples but %u output samples + max delay %u are needed",
+                d.row_samples, d.nr_samples, max_delay);
+  const uint32_t bits = family_bits(p->mode, p->bits) == 8 ? p->bits : family_bits(p->mode, p->bits);
+  const uint32_t a = dd::window_alignment_samples(bits);
+  p->win = ((k.tile_t + spread + a + 8) + 15) / 16 * 16;
+  p->smem = dd::kernel_smem_bytes(k, p->win, bits);
+  int dev_max = 0;
+  {
+    DeviceGuard g(p->device);
+    DD_CUDA(cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device),
+            "query shared memory");
+  }
+  if (p->smem > (size_t)dev_max)
+    return fail(DD_ERR_UNSUPPORTED,
+                "tile %s needs %zu bytes of shared memory (window %u samples), device allows %d; "
+                "use a configuration with fewer DMs per tile",
+                k.name, p->smem, p->win, dev_max);
+  // Upload.
+  DeviceGuard g(p->device);
+  if (p->groups.size() > p->cap_groups) {
+    if (p->d_groups) cudaFree(p->d_groups);
+    p->d_groups = nullptr;
+    DD_CUDA(cudaMalloc(&p->d_groups, std::max<size_t>(1, p->groups.size()) * sizeof(dd::GroupDesc)),
+            "allocate group table");
+    p->cap_groups = p->groups.size();
+  }
+  if (p->entries.size() > p->cap_entries || !p->d_entries) {
+    if (p->d_entries) cudaFree(p->d_entries);
+    p->d_entries = nullptr;
+    DD_CUDA(cudaMalloc(&p->d_entries, std::max<size_t>(1, p->entries.size()) * sizeof(dd::EntryDesc)),
+            "allocate entry table");
+    p->cap_entries = std::max<size_t>(1, p->entries.size());
+  }
+  if (!p->groups.empty())
+    DD_CUDA(cudaMemcpy(p->d_groups, p->groups.data(), p->groups.size() * sizeof(dd::GroupDesc),
+                       cudaMemcpyHostToDevice), "upload group table");
+  if (!p->entries.empty())
+    DD_CUDA(cudaMemcpy(p->d_entries, p->entries.data(), p->entries.size() * sizeof(dd::EntryDesc),
+                       cudaMemcpyHostToDevice), "upload entry table");
+  // The attribute is a cap shared by every plan of this kernel: set it to the
+  // device maximum so that no plan lowers it below another plan's need.
+  DD_CUDA(cudaFuncSetAttribute(k.func, cudaFuncAttributeMaxDynamicSharedMemorySize, dev_max),
+          "set kernel shared memory");
+  p->ready = true;
+  return DD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *dd_last_error(void) { return g_error.c_str(); }
+
+int dd_version(void) { return DD_ABI_VERSION; }
+
+dd_status dd_device_count(int *count) {
+  if (!count) return fail(DD_ERR_INVALID_ARGUMENT, "count is NULL");
+  *count = 0;
+  cudaError_t e = cudaGetDeviceCount(count);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    *count = 0;
+  }
+  return DD_OK;
+}
+
+uint64_t dd_pad(uint64_t value, uint64_t padding) { return pad(value, padding); }
+
+float dd_max_freq(const dd_observation *o) { return o ? max_freq(o) : 0.0f; }
+float dd_subband_min_freq(const dd_observation *o) {
+  return (o && o->nr_subbands) ? subband_min_freq(o) : 0.0f;
+}
+float dd_subband_max_freq(const dd_observation *o) {
+  return (o && o->nr_subbands) ? subband_max_freq(o) : 0.0f;
+}
+float dd_subband_bandwidth(const dd_observation *o) {
+  return (o && o->nr_subbands) ? subband_bandwidth(o) : 0.0f;
+}
+
+dd_status dd_get_shifts(const dd_observation *o, uint32_t padding, float *shifts,
+                        size_t capacity) {
+  if (!o || !shifts) return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (o->nr_channels == 0) return fail(DD_ERR_INVALID_ARGUMENT, "nr_channels is 0");
+  if (o->downsampling == 0) return fail(DD_ERR_INVALID_ARGUMENT, "downsampling is 0");
+  size_t n = pad(o->nr_channels, padding / sizeof(float));
+  if (capacity < n) return fail(DD_ERR_INVALID_ARGUMENT, "shift table needs %zu floats", n);
+  std::fill(shifts, shifts + n, 0.0f);
+  shift_table(o, o->min_freq, o->channel_bandwidth, max_freq(o), o->nr_channels, shifts);
+  return DD_OK;
+}
+
+dd_status dd_get_shifts_step_two(const dd_observation *o, uint32_t padding, float *shifts,
+                                 size_t capacity) {
+  if (!o || !shifts) return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (o->nr_subbands == 0 || o->nr_subbands > o->nr_channels)
+    return fail(DD_ERR_INVALID_ARGUMENT, "nr_subbands must be in 1..nr_channels");
+  if (o->downsampling == 0) return fail(DD_ERR_INVALID_ARGUMENT, "downsampling is 0");
+  size_t n = pad(o->nr_subbands, padding / sizeof(float));
+  if (capacity < n) return fail(DD_ERR_INVALID_ARGUMENT, "shift table needs %zu floats", n);
+  std::fill(shifts, shifts + n, 0.0f);
+  shift_table(o, subband_min_freq(o), subband_bandwidth(o), subband_max_freq(o),
+              o->nr_subbands, shifts);
+  return DD_OK;
+}
+
+dd_status dd_get_layout(const dd_observation *o, dd_mode mode, uint32_t input_bits,
+                        uint32_t padding, const float *shifts, dd_layout *layout) {
+  dd_status st = check_obs(o, mode);
+  if (st) return st;
+  if (!layout) return fail(DD_ERR_INVALID_ARGUMENT, "layout is NULL");
+  if (mode == DD_STEP_TWO) input_bits = 32;
+  if (!bits_ok(input_bits)) return fail(DD_ERR_UNSUPPORTED, "input_bits %u not supported", input_bits);
+  Dims d = dims_of(o, mode, input_bits, padding);
+  layout->input_row_bytes = d.row_bytes;
+  layout->input_bytes = d.input_bytes;
+  layout->output_row_elems = d.out_row;
+  layout->output_bytes = d.output_rows * d.out_row * sizeof(float);
+  layout->mapping_row_elems = d.mapping_row;
+  layout->zapped_elems = d.zapped_elems;
+  layout->shifts_elems = d.shift_elems;
+  layout->max_delay = 0;
+  if (shifts && d.nr_dms) {
+    uint32_t n = mode == DD_STEP_TWO ? o->nr_subbands : o->nr_channels;
+    for (uint32_t c = 0; c < n; c++) {
+      float sh = shifts[c];
+      if (mode == DD_STEP_ONE) {
+        uint32_t cps = o->nr_channels / o->nr_subbands;
+        if (c >= cps * o->nr_subbands) break;
+        volatile float rel = shifts[c] - shifts[(c / cps + 1) * cps - 1];
+        sh = rel;
+      }
+      layout->max_delay = std::max(layout->max_delay, dd::host_delay(d.first_dm, d.dm_step, d.nr_dms - 1, sh));
+    }
+  }
+  layout->required_dispersed_samples = d.nr_samples + layout->max_delay;
+  return DD_OK;
+}
+
+dd_status dd_default_conf(const dd_observation *o, dd_mode mode, uint32_t input_bits,
+                          dd_conf *conf) {
+  (void)o;
+  if (!conf) return fail(DD_ERR_INVALID_ARGUMENT, "conf is NULL");
+  if (mode == DD_STEP_TWO) input_bits = 32;
+  if (!bits_ok(input_bits)) return fail(DD_ERR_UNSUPPORTED, "input_bits %u not supported", input_bits);
+  int n = 0;
+  const dd::KernelInfo *reg = dd::kernel_registry(&n);
+  const uint32_t fb = family_bits(mode, input_bits);
+  for (int i = 0; i < n; i++)
+    if ((uint32_t)reg[i].elem_bits == fb) {
+      *conf = conf_of(reg[i]);
+      return DD_OK;
+    }
+  return fail(DD_ERR_UNSUPPORTED, "no kernel for %u-bit input", input_bits);
+}
+
+dd_status dd_conf_print(const dd_conf *c, char *text, size_t capacity) {
+  if (!c || !text || capacity == 0) return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
+  int n = snprintf(text, capacity, "%u %u %u %u %u %u %u %u %u", c->split_batches ? 1u : 0u,
+                   c->local_mem ? 1u : 0u, c->unroll, c->threads_d0, c->threads_d1, c->threads_d2,
+                   c->items_d0, c->items_d1, c->items_d2);
+  if (n < 0 || (size_t)n >= capacity) return fail(DD_ERR_INVALID_ARGUMENT, "buffer too small");
+  return DD_OK;
+}
+
+dd_status dd_read_tuned_conf(const char *path, const char *device, uint32_t nr_dms,
+                             dd_conf *conf) {
+  if (!path || !device || !conf) return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
+  std::ifstream in(path);
+  if (!in) return fail(DD_ERR_FILE, "Impossible to open %s", path);
+  std::string line;
+  unsigned lineno = 0;
+  while (std::getline(in, line)) {
+    lineno++;
+    if (line.empty() || !std::isalpha(static_cast<unsigned char>(line[0]))) continue;
+    std::istringstream ls(line);
+    std::string dev;
+    unsigned long v[10];
+    ls >> dev;
+    bool good = true;
+    for (int i = 0; i < 10 && good; i++) good = static_cast<bool>(ls >> v[i]);
+    if (!good)
+      return fail(DD_ERR_FILE, "%s:%u: expected 'device nrDMs split local unroll tD0 tD1 tD2 "
+                  "iD0 iD1 iD2'", path, lineno);
+    if (dev != device || v[0] != nr_dms) continue;
+    conf->split_batches = v[1] != 0; conf->local_mem = v[2] != 0; conf->unroll = (uint32_t)v[3];
+    conf->threads_d0 = (uint32_t)v[4]; conf->threads_d1 = (uint32_t)v[5];
+    conf->threads_d2 = (uint32_t)v[6]; conf->items_d0 = (uint32_t)v[7];
+    conf->items_d1 = (uint32_t)v[8]; conf->items_d2 = (uint32_t)v[9];
+    return DD_OK;  // the first line for (device, nrDMs) wins, as std::map::insert keeps it
+  }
+  return fail(DD_ERR_NOT_FOUND, "no entry for device '%s' and %u DMs in %s", device, nr_dms, path);
+}
+
+dd_status dd_write_tuned_conf(const char *path, const char *device, uint32_t nr_dms,
+                              const dd_conf *conf) {
+  if (!path || !device || !conf) return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (!*device || !std::isalpha(static_cast<unsigned char>(device[0])) || strchr(device, ' '))
+    return fail(DD_ERR_INVALID_ARGUMENT, "device name must start with a letter and hold no spaces");
+  char text[256];
+  dd_status st = dd_conf_print(conf, text, sizeof(text));
+  if (st) return st;
+  std::ofstream out(path, std::ios::app);
+  if (!out) return fail(DD_ERR_FILE, "Impossible to open %s", path);
+  out << device << " " << nr_dms << " " << text << "\n";
+  return out ? DD_OK : fail(DD_ERR_FILE, "write to %s failed", path);
+}
+
+dd_status dd_plan_create(dd_plan **plan, const dd_observation *o, dd_mode mode,
+                         uint32_t input_bits, uint32_t padding, const dd_conf *conf,
+                         int device) {
+  if (!plan) return fail(DD_ERR_INVALID_ARGUMENT, "plan is NULL");
+  *plan = nullptr;
+  dd_status st = check_obs(o, mode);
+  if (st) return st;
+  if (mode == DD_STEP_TWO) input_bits = 32;
+  if (!bits_ok(input_bits)) return fail(DD_ERR_UNSUPPORTED, "input_bits %u not supported", input_bits);
+  st = device_ok();
+  if (st) return st;
+  int ndev = 0;
+  cudaGetDeviceCount(&ndev);
+  if (device < 0 || device >= ndev)
+    return fail(DD_ERR_INVALID_ARGUMENT, "device %d out of range (0..%d)", device, ndev - 1);
+  dd_conf c{};
+  if (conf) c = *conf;
+  else dd_default_conf(o, mode, input_bits, &c);
+  if (c.split_batches) return fail(DD_ERR_UNSUPPORTED, "split_batches is not implemented by the reference either");
+  if (!c.local_mem) return fail(DD_ERR_UNSUPPORTED, "only local_mem=1 (staged rows) configurations are compiled");
+  const dd::KernelInfo *k = find_kernel(mode, input_bits, c);
+  if (!k) {
+    char text[128];
+    dd_conf_print(&c, text, sizeof(text));
+    return fail(DD_ERR_UNSUPPORTED, "no compiled kernel for configuration '%s' (%u-bit input)", text,
+                input_bits);
+  }
+  dd_plan *p = new dd_plan();
+  p->device = device; p->obs = *o; p->mode = mode; p->bits = input_bits; p->padding = padding;
+  p->kinfo = k;
+  p->dims = dims_of(o, mode, input_bits, padding);
+  {
+    DeviceGuard g(device);
+    cudaError_t e = cudaMalloc(&p->d_status, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(p->d_status, 0, sizeof(uint32_t));
+    if (e != cudaSuccess) {
+      delete p;
+      return cuda_fail(e, "allocate status word");
+    }
+  }
+  *plan = p;
+  return DD_OK;
+}
+
+dd_status dd_plan_set_shifts(dd_plan *p, const float *shifts, size_t n) {
+  if (!p || !shifts) return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
+  size_t need = p->mode == DD_STEP_TWO ? p->obs.nr_subbands : p->obs.nr_channels;
+  if (n < need) return fail(DD_ERR_INVALID_ARGUMENT, "shift table has %zu entries, needs %zu", n, need);
+  p->shifts.assign(shifts, shifts + need);
+  p->have_shifts = true;
+  return rebuild(p);
+}
+
+dd_status dd_plan_set_zapped(dd_plan *p, const uint32_t *zapped, size_t n) {
+  if (!p || !zapped) return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (p->mode == DD_STEP_TWO) return fail(DD_ERR_INVALID_ARGUMENT, "step two has no zapped mask");
+  if (n < p->obs.nr_channels)
+    return fail(DD_ERR_INVALID_ARGUMENT, "zapped mask has %zu entries, needs %u", n, p->obs.nr_channels);
+  p->zapped.assign(zapped, zapped + p->obs.nr_channels);
+  return rebuild(p);
+}
+
+dd_status dd_plan_set_beam_mapping(dd_plan *p, const uint32_t *mapping, size_t n) {
+  if (!p || !mapping) return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (p->mode == DD_STEP_ONE) return fail(DD_ERR_INVALID_ARGUMENT, "step one has no beam mapping");
+  size_t need = (size_t)p->obs.nr_synthesized_beams * p->dims.mapping_row;
+  if (n < need) return fail(DD_ERR_INVALID_ARGUMENT, "beam mapping has %zu entries, needs %zu", n, need);
+  p->mapping.assign(mapping, mapping + need);
+  return rebuild(p);
+}
+
+dd_status dd_plan_run(dd_plan *p, const void *d_input, float *d_output, void *stream) {
+  if (!p) return fail(DD_ERR_INVALID_ARGUMENT, "plan is NULL");
+  if (!p->ready)
+    return fail(DD_ERR_INVALID_ARGUMENT, p->have_shifts ? "plan tables are invalid: %s"
+                                                        : "plan has no shift table%s",
+                p->have_shifts ? g_error.c_str() : "");
+  const uint64_t tiles = (uint64_t)p->nr_groups * p->tiles_d * p->tiles_t;
+  if (tiles == 0) return DD_OK;
+  if (!d_input || !d_output) return fail(DD_ERR_INVALID_ARGUMENT, "NULL data pointer");
+  if (tiles > 0x7fffffffull) return fail(DD_ERR_UNSUPPORTED, "problem has %llu tiles", (unsigned long long)tiles);
+  const Dims &d = p->dims;
+  dd::ProblemDesc P{};
+  P.in = static_cast<const uint8_t *>(d_input);
+  P.out = d_output;
+  P.groups = p->d_groups;
+  P.entries = p->d_entries;
+  P.status = p->d_status;
+  P.row_bytes = d.row_bytes;
+  P.out_dm_stride = p->out_dm_stride;
+  P.nr_groups = p->nr_groups;
+  P.nr_dms = d.nr_dms;
+  P.nr_samples = d.nr_samples;
+  P.bits = p->mode == DD_STEP_TWO ? 32 : p->bits;
+  P.first_dm = d.first_dm;
+  P.dm_step = d.dm_step;
+  P.win_samples = p->win;
+  P.tiles_t = p->tiles_t;
+  P.tiles_d = p->tiles_d;
+  P.tma = (d.row_bytes % 16 == 0 && reinterpret_cast<uintptr_t>(d_input) % 16 == 0) ? 1u : 0u;
+  P.out_vec4 = (d.out_row % 4 == 0 && reinterpret_cast<uintptr_t>(d_output) % 16 == 0) ? 1u : 0u;
+  DeviceGuard g(p->device);
+  if (!g.ok) return fail(DD_ERR_CUDA, "cannot select device %d", p->device);
+  p->kinfo->launch(P, (unsigned)tiles, p->smem, static_cast<cudaStream_t>(stream));
+  DD_CUDA(cudaGetLastError(), "launch dedispersion kernel");
+  return DD_OK;
+}
+
+dd_status dd_plan_check(dd_plan *p, void *stream) {
+  if (!p) return fail(DD_ERR_INVALID_ARGUMENT, "plan is NULL");
+  DeviceGuard g(p->device);
+  DD_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)), "synchronize stream");
+  uint32_t status = 0;
+  DD_CUDA(cudaMemcpy(&status, p->d_status, sizeof(status), cudaMemcpyDeviceToHost), "read status");
+  if (status) {
+    DD_CUDA(cudaMemset(p->d_status, 0, sizeof(uint32_t)), "reset status");
+    if (status & dd::kStatusTimeout)
+      return fail(DD_ERR_TIMEOUT, "a bounded wait for a staged row ran out on the device");
+    return fail(DD_ERR_CUDA, "device status 0x%x", status);
+  }
+  return DD_OK;
+}
+
+dd_status dd_plan_launches(const dd_plan *p, uint32_t *launches) {
+  if (!p || !launches) return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
+  *launches = ((uint64_t)p->nr_groups * p->tiles_d * p->tiles_t) ? 1u : 0u;
+  return DD_OK;
+}
+
+dd_status dd_plan_get_conf(const dd_plan *p, dd_conf *conf) {
+  if (!p || !conf) return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
+  *conf = conf_of(*p->kinfo);
+  return DD_OK;
+}
+
+dd_status dd_plan_destroy(dd_plan *p) {
+  if (!p) return DD_OK;
+  {
+    DeviceGuard g(p->device);
+    if (p->d_groups) cudaFree(p->d_groups);
+    if (p->d_entries) cudaFree(p->d_entries);
+    if (p->d_status) cudaFree(p->d_status);
+  }
+  delete p;
+  return DD_OK;
+}
+
+}  // extern "C"
+
+// ---- synchronous host-buffer calls ----------------------------------------
+
+namespace {
+
+// Per-thread cache of the last plan and device buffers of the synchronous
+// calls, so that repeated calls on one geometry only copy and launch.
+struct SyncCache {
+  dd_plan *plan = nullptr;
+  dd_observation obs{};
+  dd_mode mode = DD_SINGLE_STEP;
+  uint32_t bits = 0, padding = 0;
+  std::vector<float> shifts;
+  std::vector<uint32_t> zapped, mapping;
+  void *d_in = nullptr;
+  float *d_out = nullptr;
+  size_t cap_in = 0, cap_out = 0;
+  cudaStream_t stream = nullptr;
+  ~SyncCache() {
+    if (plan) dd_plan_destroy(plan);
+    if (d_in) cudaFree(d_in);
+    if (d_out) cudaFree(d_out);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+thread_local SyncCache g_sync;
+
+dd_status run_sync(const dd_observation *o, dd_mode mode, const uint32_t *zapped,
+                   const uint32_t *mapping, const void *input, float *output,
+                   const float *shifts, uint32_t padding, uint32_t bits) {
+  dd_status st = check_obs(o, mode);
+  if (st) return st;
+  if (!input || !output || !shifts) return fail(DD_ERR_INVALID_ARGUMENT, "NULL data pointer");
+  if (mode != DD_STEP_TWO && !zapped) return fail(DD_ERR_INVALID_ARGUMENT, "zapped mask is NULL");
+  if (mode != DD_STEP_ONE && !mapping) return fail(DD_ERR_INVALID_ARGUMENT, "beam mapping is NULL");
+  if (mode == DD_STEP_TWO) bits = 32;
+  st = device_ok();
+  if (st) return st;
+  SyncCache &c = g_sync;
+  const bool same_geom = c.plan && c.mode == mode && c.bits == bits && c.padding == padding &&
+                         std::memcmp(&c.obs, o, sizeof(*o)) == 0;
+  if (!same_geom) {
+    if (c.plan) dd_plan_destroy(c.plan);
+    c.plan = nullptr;
+    c.shifts.clear(); c.zapped.clear(); c.mapping.clear();
+    st = dd_plan_create(&c.plan, o, mode, bits, padding, nullptr, 0);
+    if (st) return st;
+    c.obs = *o; c.mode = mode; c.bits = bits; c.padding = padding;
+  }
+  const Dims &d = c.plan->dims;
+  const size_t nsh = mode == DD_STEP_TWO ? o->nr_subbands : o->nr_channels;
+  bool dirty = false;
+  if (c.shifts.size() != nsh || std::memcmp(c.shifts.data(), shifts, nsh * 4)) {
+    c.shifts.assign(shifts, shifts + nsh);
+    c.plan->shifts = c.shifts;
+    c.plan->have_shifts = true;
+    dirty = true;
+  }
+  if (mode != DD_STEP_TWO &&
+      (c.zapped.size() != o->nr_channels || std::memcmp(c.zapped.data(), zapped, o->nr_channels * 4))) {
+    c.zapped.assign(zapped, zapped + o->nr_channels);
+    c.plan->zapped = c.zapped;
+    dirty = true;
+  }
+  if (mode != DD_STEP_ONE) {
+    size_t nm = (size_t)o->nr_synthesized_beams * d.mapping_row;
+    if (c.mapping.size() != nm || std::memcmp(c.mapping.data(), mapping, nm * 4)) {
+      c.mapping.assign(mapping, mapping + nm);
+      c.plan->mapping = c.mapping;
+      dirty = true;
+    }
+  }
+  if (dirty) {
+    st = rebuild(c.plan);
+    if (st) {
+      c.shifts.clear();
+      return st;
+    }
+  }
+  DeviceGuard g(0);
+  if (!c.stream) DD_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking), "create stream");
+  const size_t in_bytes = d.input_bytes;
+  const size_t out_bytes = d.output_rows * d.out_row * sizeof(float);
+  if (in_bytes > c.cap_in) {
+    if (c.d_in) cudaFree(c.d_in);
+    c.d_in = nullptr; c.cap_in = 0;
+    DD_CUDA(cudaMalloc(&c.d_in, in_bytes), "allocate device input");
+    c.cap_in = in_bytes;
+  }
+  if (out_bytes > c.cap_out) {
+    if (c.d_out) cudaFree(c.d_out);
+    c.d_out = nullptr; c.cap_out = 0;
+    DD_CUDA(cudaMalloc(&c.d_out, out_bytes), "allocate device output");
+    c.cap_out = out_bytes;
+  }
+  if (in_bytes)
+    DD_CUDA(cudaMemcpyAsync(c.d_in, input, in_bytes, cudaMemcpyHostToDevice, c.stream), "copy input");
+  st = dd_plan_run(c.plan, c.d_in, c.d_out, c.stream);
+  if (st) return st;
+  if (d.output_rows && d.nr_samples)
+    DD_CUDA(cudaMemcpy2DAsync(output, d.out_row * sizeof(float), c.d_out, d.out_row * sizeof(float),
+                              (size_t)d.nr_samples * sizeof(float), d.output_rows,
+                              cudaMemcpyDeviceToHost, c.stream),
+            "copy output");
+  return dd_plan_check(c.plan, c.stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+dd_status dd_dedispersion(const dd_observation *o, const uint32_t *zapped,
+                          const uint32_t *beam_mapping, const void *input, float *output,
+                          const float *shifts, uint32_t padding, uint32_t input_bits) {
+  return run_sync(o, DD_SINGLE_STEP, zapped, beam_mapping, input, output, shifts, padding,
+                  input_bits);
+}
+
+dd_status dd_subband_dedispersion_step_one(const dd_observation *o, const uint32_t *zapped,
+                                           const void *input, float *output, const float *shifts,
+                                           uint32_t padding, uint32_t input_bits) {
+  return run_sync(o, DD_STEP_ONE, zapped, nullptr, input, output, shifts, padding, input_bits);
+}
+
+dd_status dd_subband_dedispersion_step_two(const dd_observation *o, const uint32_t *beam_mapping,
+                                           const float *input, float *output, const float *shifts,
+                                           uint32_t padding) {
+  return run_sync(o, DD_STEP_TWO, nullptr, beam_mapping, input, output, shifts, padding, 32);
+}
+
+}  // extern "C"

@@ -1,0 +1,538 @@
+// dd_device.cuh -- sm_103a device code of the dedispersion tile kernels.
+//
+// One CTA computes one tile: TILE_D DMs x TILE_T output samples of one output
+// group (dd_internal.h).  For every input row of the group (a live channel,
+// or a subband in step two) the CTA needs the row window
+//
+//   [t0 + delay(row, d0), t0 + TILE_T + delay(row, d0 + TILE_D - 1))
+//
+// It stages CH rows per pipeline stage into shared memory with bulk async
+// copies (cp.async.bulk, the 1-D TMA path; no multicast), completion tracked
+// by an mbarrier per staging slot, three slots in flight.  The device twin of
+// the reference's local-memory kernel (include/Dedispersion.hpp:225-309),
+// which copies each channel's window into __local memory.
+//
+// Two tile families:
+//
+// * swar8 (input of 1, 2, 4 or 8 bits).  Rows are expanded to one byte per
+//   sample while staged and kept as four copies shifted by 0..3 bytes, so a
+//   window read at any sample offset is one aligned 32-bit load.  A loaded
+//   word holds four consecutive samples; two byte permutes spread them over
+//   two registers of two 16-bit lanes, and integer adds accumulate two
+//   samples per lane pair (SWAR).  16-bit lanes are flushed into 32-bit
+//   totals every 256 rows (256 * 255 < 2^16), so sums are exact integers.
+//
+// * scalar (16-bit or float input, and step two).  Element loads at any
+//   offset; 16-bit input accumulates in uint32, float input in float32 in row
+//   order, the reference's own order (include/Dedispersion.hpp:79-104), so
+//   float results are identical to the reference's.
+//
+// Every wait on a bulk copy is bounded (kWaitNs); when one runs out the CTA
+// sets kStatusTimeout in the problem's status word, waits a bounded time for
+// its other copies, and returns.
+#pragma once
+
+#include <cstdint>
+
+#include "dd_internal.h"
+
+namespace dd {
+
+constexpr int kNRaw = 3;                            // staging slots
+constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per bulk copy
+constexpr unsigned long long kDrainNs = 50000000ull;   // 50 ms when aborting
+
+__host__ __device__ inline uint32_t round_up(uint32_t v, uint32_t m) {
+  return (v + m - 1) / m * m;
+}
+
+// Samples per 16 bytes of a row: the alignment of a staged window's start.
+__host__ __device__ inline uint32_t align_samples(uint32_t bits) {
+  return bits <= 8 ? 16u * (8u / bits) : 16u / (bits / 8u);
+}
+
+// Shared memory layout of one CTA (byte offsets from the dynamic base).
+struct SmemLayout {
+  uint32_t raw_bytes;   // one staged row in a raw slot
+  uint32_t copy_words;  // words of one shifted copy (swar8)
+  uint32_t off_bar, off_wstart, off_table, off_raw, off_copy, total;
+};
+
+__host__ __device__ inline SmemLayout make_layout(int family, uint32_t win,
+                                                  uint32_t bits, int ch,
+                                                  int tile_d) {
+  SmemLayout L;
+  const uint32_t a = align_samples(bits);
+  if (family == kFamilySwar8) {
+    L.raw_bytes = round_up((win + a) * bits / 8u, 16u);
+    L.copy_words = win / 4u;
+  } else {
+    L.raw_bytes = round_up(win * (bits / 8u), 16u);
+    L.copy_words = 0;
+  }
+  L.off_bar = 0;
+  L.off_wstart = 64;
+  L.off_table = round_up(L.off_wstart + kNRaw * ch * 4u, 128u);
+  L.off_raw = round_up(L.off_table + 2u * ch * tile_d * 4u, 128u);
+  L.off_copy = round_up(L.off_raw + kNRaw * ch * L.raw_bytes, 128u);
+  L.total = L.off_copy + 2u * ch * 4u * L.copy_words * 4u;
+  return L;
+}
+
+// ---- PTX wrappers ---------------------------------------------------------
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar,
+                                                      uint32_t bytes) {
+  asm volatile(
+      "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+          smem_addr(bar)),
+      "r"(bytes)
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait for the phase with `parity` to complete.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
+                                          unsigned long long limit_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long start = global_ns();
+  for (;;) {
+#pragma unroll 1
+    for (int i = 0; i < 32; ++i)
+      if (mbar_try_wait(bar, parity)) return true;
+    if (global_ns() - start > limit_ns) return false;
+  }
+}
+
+// 1-D bulk copy global -> shared, completing `bytes` on `bar`.  Both
+// addresses 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src,
+                                         uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+// The reference's per-row delay, (uint)((firstDM + dm * dmStep) * shift),
+// with every operation rounded as the CPU rounds it (no contraction).
+__device__ __forceinline__ uint32_t dev_delay(float first, float step,
+                                              uint32_t dm, float shift) {
+  const float v = __fadd_rn(first, __fmul_rn(__uint2float_rn(dm), step));
+  return __float2uint_rz(__fmul_rn(v, shift));
+}
+
+// Samples 4k..4k+3 of a packed sub-byte row, one per byte, zero-extended.
+// Sample n lives in byte n / (8 / bits) at bit (n % (8 / bits)) * bits.
+__device__ __forceinline__ uint32_t expand_word(const uint8_t *row, uint32_t k,
+                                                uint32_t bits) {
+  uint32_t v;
+  if (bits == 4)
+    v = reinterpret_cast<const uint16_t *>(row)[k];
+  else if (bits == 2)
+    v = row[k];
+  else
+    v = (row[k >> 1] >> ((k & 1u) * 4u)) & 0xFu;
+  const uint32_t m = (1u << bits) - 1u;
+  uint32_t out = 0;
+#pragma unroll
+  for (int s = 0; s < 4; ++s) out |= ((v >> (s * bits)) & m) << (8 * s);
+  return out;
+}
+
+// ---- staging shared by both families --------------------------------------
+
+struct StageCtx {
+  uint64_t *bars;
+  uint32_t *wstart;
+  uint8_t *raw;
+  uint32_t raw_bytes;
+};
+
+// Issue stage `s` (global stage index gs) of group G: lanes 0..CH-1 of the
+// calling warp each stage one row.  Every lane < CH arrives once.
+template <int CH>
+__device__ __forceinline__ void issue_stage(const ProblemDesc &P,
+                                            const GroupDesc &G,
+                                            const StageCtx &S, uint32_t s,
+                                            uint32_t gs, uint32_t t0,
+                                            uint32_t d0, int lane) {
+  if (lane >= CH) return;
+  const uint32_t slot = gs % kNRaw;
+  uint64_t *bar = S.bars + slot;
+  const uint32_t e = s * CH + lane;
+  if (e >= G.entry_count) {
+    mbar_arrive(bar);
+    return;
+  }
+  const EntryDesc E = P.entries[G.entry_begin + e];
+  const uint32_t a = align_samples(P.bits);
+  const uint32_t ws = (t0 + dev_delay(P.first_dm, P.dm_step, d0, E.shift)) / a * a;
+  S.wstart[slot * CH + lane] = ws;
+  if (P.tma) {
+    const uint64_t boff = P.bits <= 8 ? (uint64_t)ws * P.bits / 8u
+                                      : (uint64_t)ws * (P.bits / 8u);
+    const uint64_t avail = P.row_bytes - boff;
+    const uint32_t bytes =
+        avail < S.raw_bytes ? static_cast<uint32_t>(avail) : S.raw_bytes;
+    mbar_arrive_expect_tx(bar, bytes);
+    bulk_g2s(S.raw + (slot * CH + lane) * S.raw_bytes,
+             P.in + E.row_offset + boff, bytes, bar);
+  } else {
+    mbar_arrive(bar);
+  }
+}
+
+// Without bulk copies (unaligned rows): the CTA copies the windows of one
+// stage byte by byte; bytes past the row end read as zero.
+template <int CH, int TY>
+__device__ __forceinline__ void copy_stage_plain(const ProblemDesc &P,
+                                                 const GroupDesc &G,
+                                                 const StageCtx &S, uint32_t s,
+                                                 uint32_t slot, uint32_t cnt) {
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (uint32_t ch = ty; ch < cnt; ch += TY) {
+    const EntryDesc E = P.entries[G.entry_begin + s * CH + ch];
+    const uint32_t ws = S.wstart[slot * CH + ch];
+    const uint64_t boff = P.bits <= 8 ? (uint64_t)ws * P.bits / 8u
+                                      : (uint64_t)ws * (P.bits / 8u);
+    const uint8_t *src = P.in + E.row_offset;
+    uint8_t *dst = S.raw + (slot * CH + ch) * S.raw_bytes;
+    for (uint32_t b = tx; b < S.raw_bytes; b += 32)
+      dst[b] = (boff + b < P.row_bytes) ? src[boff + b] : 0;
+  }
+}
+
+// Abort path: wait a bounded time for stages [from, to) still in flight.
+__device__ __forceinline__ void drain_stages(const StageCtx &S, uint32_t sc,
+                                             uint32_t from, uint32_t to) {
+  for (uint32_t s = from; s < to; ++s) {
+    const uint32_t gs = sc + s;
+    (void)mbar_wait(S.bars + gs % kNRaw, (gs / kNRaw) & 1u, kDrainNs);
+  }
+}
+
+// ---- swar8 tile -----------------------------------------------------------
+
+// Computes one tile; returns false if the CTA must stop (timeout).  `sc`
+// counts the CTA's stages across tiles (mbarrier phase bookkeeping).
+template <int NW, int NDT, int TY, int CH>
+__device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
+                                           const GroupDesc &G, uint32_t dtile,
+                                           uint32_t ttile, uint8_t *smem,
+                                           const SmemLayout &L, uint32_t &sc) {
+  constexpr int kTileT = 32 * NW * 4;
+  constexpr int kTileD = TY * NDT;
+  constexpr int kThreads = 32 * TY;
+  static_assert(CH <= 32 && CH % 2 == 0, "CH rows per stage, even, <= 32");
+  const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+  const uint32_t t0 = ttile * kTileT, d0 = dtile * kTileD;
+  const uint32_t K = G.entry_count;
+  const uint32_t nst = (K + CH - 1) / CH;
+  const uint32_t cw = L.copy_words;
+  StageCtx S;
+  S.bars = reinterpret_cast<uint64_t *>(smem + L.off_bar);
+  S.wstart = reinterpret_cast<uint32_t *>(smem + L.off_wstart);
+  S.raw = smem + L.off_raw;
+  S.raw_bytes = L.raw_bytes;
+  uint32_t *table = reinterpret_cast<uint32_t *>(smem + L.off_table);
+  uint32_t *copies = reinterpret_cast<uint32_t *>(smem + L.off_copy);
+
+  if (ty == 0) {
+    const uint32_t pro = nst < (uint32_t)kNRaw ? nst : (uint32_t)kNRaw;
+    for (uint32_t s = 0; s < pro; ++s)
+      issue_stage<CH>(P, G, S, s, sc + s, t0, d0, tx);
+  }
+
+  uint32_t lo[NDT][NW], hi[NDT][NW], tot[NDT][NW][4];
+#pragma unroll
+  for (int j = 0; j < NDT; ++j)
+#pragma unroll
+    for (int i = 0; i < NW; ++i) {
+      lo[j][i] = hi[j][i] = 0;
+      tot[j][i][0] = tot[j][i][1] = tot[j][i][2] = tot[j][i][3] = 0;
+    }
+  uint32_t since = 0;
+
+  for (uint32_t s = 0; s < nst; ++s) {
+    const uint32_t gs = sc + s, slot = gs % kNRaw, area = gs & 1u;
+    const uint32_t cnt = (K - s * CH) < (uint32_t)CH ? (K - s * CH) : CH;
+    const bool ok = mbar_wait(S.bars + slot, (gs / kNRaw) & 1u, kWaitNs);
+    if (!P.tma) {
+      copy_stage_plain<CH, TY>(P, G, S, s, slot, cnt);
+      __syncthreads();
+    }
+    // Expand to bytes and write the four shifted copies of each row.
+    uint32_t *ac = copies + area * (CH * 4u * cw);
+    for (uint32_t ch = ty; ch < cnt; ch += TY) {
+      const uint8_t *r = S.raw + (slot * CH + ch) * S.raw_bytes;
+      uint32_t *dst = ac + ch * 4u * cw;
+      for (uint32_t k = tx; k < cw; k += 32) {
+        uint32_t w0, w1;
+        if (P.bits == 8) {
+          w0 = reinterpret_cast<const uint32_t *>(r)[k];
+          w1 = reinterpret_cast<const uint32_t *>(r)[k + 1];
+        } else {
+          w0 = expand_word(r, k, P.bits);
+          w1 = expand_word(r, k + 1, P.bits);
+        }
+        dst[k] = w0;
+        dst[cw + k] = __funnelshift_r(w0, w1, 8);
+        dst[2 * cw + k] = __funnelshift_r(w0, w1, 16);
+        dst[3 * cw + k] = __funnelshift_r(w0, w1, 24);
+      }
+    }
+    // Word index of (row, DM) in the copy area: copy (o & 3), word (o >> 2).
+    uint32_t *tb = table + area * (CH * kTileD);
+    for (uint32_t idx = tid; idx < cnt * kTileD; idx += kThreads) {
+      const uint32_t ch = idx / kTileD, j = idx % kTileD;
+      const uint32_t d = (d0 + j) < P.nr_dms ? (d0 + j) : (P.nr_dms - 1);
+      const float sh = P.entries[G.entry_begin + s * CH + ch].shift;
+      const uint32_t o = t0 + dev_delay(P.first_dm, P.dm_step, d, sh) -
+                         S.wstart[slot * CH + ch];
+      tb[idx] = ch * 4u * cw + (o & 3u) * cw + (o >> 2);
+    }
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) atomicOr(P.status, kStatusTimeout);
+      const uint32_t last = (s + kNRaw) < nst ? (s + kNRaw) : nst;
+      drain_stages(S, sc, s, last);
+      return false;
+    }
+    if (ty == 0 && s + kNRaw < nst)
+      issue_stage<CH>(P, G, S, s + kNRaw, gs + kNRaw, t0, d0, tx);
+
+    if (since + cnt > 256u) {
+#pragma unroll
+      for (int j = 0; j < NDT; ++j)
+#pragma unroll
+        for (int i = 0; i < NW; ++i) {
+          tot[j][i][0] += lo[j][i] & 0xFFFFu;
+          tot[j][i][1] += lo[j][i] >> 16;
+          tot[j][i][2] += hi[j][i] & 0xFFFFu;
+          tot[j][i][3] += hi[j][i] >> 16;
+          lo[j][i] = hi[j][i] = 0;
+        }
+      since = 0;
+    }
+    since += cnt;
+
+    const uint32_t *tbt = tb + ty * NDT;
+    uint32_t ch = 0;
+    for (; ch + 1 < cnt; ch += 2) {
+      uint32_t b1[NDT], b2[NDT];
+#pragma unroll
+      for (int j = 0; j < NDT; ++j) {
+        b1[j] = tbt[ch * kTileD + j] + tx;
+        b2[j] = tbt[(ch + 1) * kTileD + j] + tx;
+      }
+#pragma unroll
+      for (int j = 0; j < NDT; ++j)
+#pragma unroll
+        for (int i = 0; i < NW; ++i) {
+          const uint32_t w1 = ac[b1[j] + 32 * i];
+          const uint32_t w2 = ac[b2[j] + 32 * i];
+          lo[j][i] += __byte_perm(w1, 0, 0x4140) + __byte_perm(w2, 0, 0x4140);
+          hi[j][i] += __byte_perm(w1, 0, 0x4342) + __byte_perm(w2, 0, 0x4342);
+        }
+    }
+    if (ch < cnt) {
+#pragma unroll
+      for (int j = 0; j < NDT; ++j) {
+        const uint32_t b = tbt[ch * kTileD + j] + tx;
+#pragma unroll
+        for (int i = 0; i < NW; ++i) {
+          const uint32_t w = ac[b + 32 * i];
+          lo[j][i] += __byte_perm(w, 0, 0x4140);
+          hi[j][i] += __byte_perm(w, 0, 0x4342);
+        }
+      }
+    }
+  }
+  sc += nst;
+
+#pragma unroll
+  for (int j = 0; j < NDT; ++j) {
+    const uint32_t d = d0 + ty * NDT + j;
+    if (d >= P.nr_dms) continue;
+    float *orow = P.out + G.out_offset + (uint64_t)d * P.out_dm_stride;
+#pragma unroll
+    for (int i = 0; i < NW; ++i) {
+      const uint32_t v0 = tot[j][i][0] + (lo[j][i] & 0xFFFFu);
+      const uint32_t v1 = tot[j][i][1] + (lo[j][i] >> 16);
+      const uint32_t v2 = tot[j][i][2] + (hi[j][i] & 0xFFFFu);
+      const uint32_t v3 = tot[j][i][3] + (hi[j][i] >> 16);
+      const uint32_t t = t0 + 4u * (tx + 32u * i);
+      if (P.out_vec4 && t + 3u < P.nr_samples) {
+        *reinterpret_cast<float4 *>(orow + t) =
+            make_float4((float)v0, (float)v1, (float)v2, (float)v3);
+      } else {
+        if (t < P.nr_samples) orow[t] = (float)v0;
+        if (t + 1u < P.nr_samples) orow[t + 1] = (float)v1;
+        if (t + 2u < P.nr_samples) orow[t + 2] = (float)v2;
+        if (t + 3u < P.nr_samples) orow[t + 3] = (float)v3;
+      }
+    }
+  }
+  return true;
+}
+
+// ---- scalar tile ----------------------------------------------------------
+
+template <typename T>
+struct ScalarAcc;
+template <>
+struct ScalarAcc<uint16_t> {
+  using type = uint32_t;
+};
+template <>
+struct ScalarAcc<float> {
+  using type = float;
+};
+
+template <typename T, int NS, int NDT, int TY, int CH>
+__device__ __forceinline__ bool scalar_tile(const ProblemDesc &P,
+                                            const GroupDesc &G, uint32_t dtile,
+                                            uint32_t ttile, uint8_t *smem,
+                                            const SmemLayout &L, uint32_t &sc) {
+  using Acc = typename ScalarAcc<T>::type;
+  constexpr int kTileT = 32 * NS;
+  constexpr int kTileD = TY * NDT;
+  constexpr int kThreads = 32 * TY;
+  constexpr int kAhead = kNRaw - 1;  // raw slots are read by compute
+  static_assert(CH <= 32, "CH rows per stage <= 32");
+  const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+  const uint32_t t0 = ttile * kTileT, d0 = dtile * kTileD;
+  const uint32_t K = G.entry_count;
+  const uint32_t nst = (K + CH - 1) / CH;
+  const uint32_t slot_elems = L.raw_bytes / sizeof(T);
+  StageCtx S;
+  S.bars = reinterpret_cast<uint64_t *>(smem + L.off_bar);
+  S.wstart = reinterpret_cast<uint32_t *>(smem + L.off_wstart);
+  S.raw = smem + L.off_raw;
+  S.raw_bytes = L.raw_bytes;
+  uint32_t *table = reinterpret_cast<uint32_t *>(smem + L.off_table);
+  const T *rawt = reinterpret_cast<const T *>(S.raw);
+
+  if (ty == 0) {
+    const uint32_t pro = nst < (uint32_t)kAhead ? nst : (uint32_t)kAhead;
+    for (uint32_t s = 0; s < pro; ++s)
+      issue_stage<CH>(P, G, S, s, sc + s, t0, d0, tx);
+  }
+
+  Acc acc[NDT][NS];
+#pragma unroll
+  for (int j = 0; j < NDT; ++j)
+#pragma unroll
+    for (int i = 0; i < NS; ++i) acc[j][i] = Acc(0);
+
+  for (uint32_t s = 0; s < nst; ++s) {
+    const uint32_t gs = sc + s, slot = gs % kNRaw, area = gs & 1u;
+    const uint32_t cnt = (K - s * CH) < (uint32_t)CH ? (K - s * CH) : CH;
+    const bool ok = mbar_wait(S.bars + slot, (gs / kNRaw) & 1u, kWaitNs);
+    if (!P.tma) {
+      copy_stage_plain<CH, TY>(P, G, S, s, slot, cnt);
+      __syncthreads();
+    }
+    uint32_t *tb = table + area * (CH * kTileD);
+    for (uint32_t idx = tid; idx < cnt * kTileD; idx += kThreads) {
+      const uint32_t ch = idx / kTileD, j = idx % kTileD;
+      const uint32_t d = (d0 + j) < P.nr_dms ? (d0 + j) : (P.nr_dms - 1);
+      const float sh = P.entries[G.entry_begin + s * CH + ch].shift;
+      const uint32_t o = t0 + dev_delay(P.first_dm, P.dm_step, d, sh) -
+                         S.wstart[slot * CH + ch];
+      tb[idx] = (slot * CH + ch) * slot_elems + o;
+    }
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) atomicOr(P.status, kStatusTimeout);
+      const uint32_t last = (s + kAhead) < nst ? (s + kAhead) : nst;
+      drain_stages(S, sc, s, last);
+      return false;
+    }
+    if (ty == 0 && s + kAhead < nst)
+      issue_stage<CH>(P, G, S, s + kAhead, gs + kAhead, t0, d0, tx);
+
+    const uint32_t *tbt = tb + ty * NDT;
+    for (uint32_t ch = 0; ch < cnt; ++ch) {
+      uint32_t b[NDT];
+#pragma unroll
+      for (int j = 0; j < NDT; ++j) b[j] = tbt[ch * kTileD + j] + tx;
+#pragma unroll
+      for (int j = 0; j < NDT; ++j)
+#pragma unroll
+        for (int i = 0; i < NS; ++i) acc[j][i] += Acc(rawt[b[j] + 32 * i]);
+    }
+  }
+  sc += nst;
+
+#pragma unroll
+  for (int j = 0; j < NDT; ++j) {
+    const uint32_t d = d0 + ty * NDT + j;
+    if (d >= P.nr_dms) continue;
+    float *orow = P.out + G.out_offset + (uint64_t)d * P.out_dm_stride;
+#pragma unroll
+    for (int i = 0; i < NS; ++i) {
+      const uint32_t t = t0 + tx + 32u * i;
+      if (t < P.nr_samples) orow[t] = (float)acc[j][i];
+    }
+  }
+  return true;
+}
+
+// Split a linear tile index into (group, DM tile, time tile); time fastest.
+__device__ __forceinline__ void decode_tile(const ProblemDesc &P,
+                                            uint32_t tile, uint32_t &g,
+                                            uint32_t &dtile, uint32_t &ttile) {
+  ttile = tile % P.tiles_t;
+  const uint32_t rest = tile / P.tiles_t;
+  dtile = rest % P.tiles_d;
+  g = rest / P.tiles_d;
+}
+
+__device__ __forceinline__ void init_barriers(uint8_t *smem,
+                                              const SmemLayout &L, int ch) {
+  if (threadIdx.x == 0) {
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L.off_bar);
+    for (int r = 0; r < kNRaw; ++r) mbar_init(bars + r, ch);
+    fence_mbar_init();
+  }
+  __syncthreads();
+}
+
+}  // namespace dd

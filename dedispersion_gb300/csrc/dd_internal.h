@@ -1,0 +1,106 @@
+// dd_internal.h -- descriptors shared by the host library and the kernels.
+//
+// A dedispersion problem is a set of output groups.  Each group sums a list
+// of input rows (its live channels, or its subbands in step two), each with
+// its own delay per unit DM, into a [DM][sample] block of the output:
+//
+//   out[g.out_offset + dm * out_dm_stride + t] =
+//       sum_k in_row(g, k)[t + (uint)((first_dm + dm * dm_step) * shift_k)]
+//
+// Single step (include/Dedispersion.hpp:70-109): group = synthesized beam,
+//   rows = non-zapped channels of the mapped beam.
+// Step one (include/Dedispersion.hpp:111-153): group = (beam, subband),
+//   rows = non-zapped channels of the subband, shift relative to the
+//   subband's last channel.
+// Step two (include/Dedispersion.hpp:155-176): group = (synthesized beam,
+//   step-one DM), rows = the subbands of the step-one output.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace dd {
+
+// One output group.
+struct GroupDesc {
+  uint32_t entry_begin;  // first entry of this group in the entry table
+  uint32_t entry_count;  // rows summed (0: the group's output is all zero)
+  uint64_t out_offset;   // float offset of (dm 0, sample 0) of the group
+};
+
+// One input row of a group.
+struct EntryDesc {
+  uint64_t row_offset;  // byte offset of the row from the input base
+  float shift;          // delay in samples per unit DM
+  uint32_t reserved;
+};
+
+// Device status word bits, set with atomicOr by a kernel.
+enum : uint32_t {
+  kStatusTimeout = 1u,  // a bounded wait on a bulk copy ran out
+};
+
+// Everything a kernel needs to compute one problem.
+struct ProblemDesc {
+  const uint8_t *in;
+  float *out;
+  const GroupDesc *groups;
+  const EntryDesc *entries;
+  uint32_t *status;
+  uint64_t row_bytes;      // input row pitch in bytes (also the clamp)
+  uint64_t out_dm_stride;  // floats between consecutive DM rows of a group
+  uint32_t nr_groups;
+  uint32_t nr_dms;
+  uint32_t nr_samples;     // output samples per DM row
+  uint32_t bits;           // 1, 2, 4, 8, 16 or 32 (float)
+  float first_dm;
+  float dm_step;
+  uint32_t win_samples;    // samples staged per row and tile
+  uint32_t tiles_t;        // time tiles per group
+  uint32_t tiles_d;        // DM tiles per group
+  uint32_t tma;            // 1: rows staged by bulk async copies
+  uint32_t out_vec4;       // 1: float4 stores are aligned
+  uint32_t reserved;
+};
+
+// One entry of the kernel registry: a compiled tile configuration.
+struct KernelInfo {
+  const char *name;
+  int family;       // kFamilySwar8 or kFamilyScalar
+  int elem_bits;    // swar8: 8 (covers 1/2/4/8); scalar: 16 or 32
+  int items_t;      // samples per thread
+  int items_d;      // DMs per thread
+  int warps_d;      // warps along the DM axis
+  int channels;     // rows per pipeline stage
+  int threads;
+  int tile_t;       // samples per tile
+  int tile_d;       // DMs per tile
+  const void *func;
+  void (*launch)(const ProblemDesc &, unsigned grid, size_t smem,
+                 cudaStream_t stream);
+};
+
+enum { kFamilySwar8 = 0, kFamilyScalar = 1 };
+
+// Registry of compiled configurations (dd_kernels.cu).
+const KernelInfo *kernel_registry(int *count);
+// Dynamic shared memory bytes of a configuration for a window size.
+size_t kernel_smem_bytes(const KernelInfo &k, uint32_t win_samples,
+                         uint32_t bits);
+// Samples a window must hold beyond the tile for row alignment.
+uint32_t window_alignment_samples(uint32_t bits);
+
+// Delay of a row for one DM, in the reference's float order
+// ((firstDM + dm * dmStep) * shift, truncated; include/Dedispersion.hpp:81).
+// Host version; the device version is in dd_device.cuh.
+inline uint32_t host_delay(float first_dm, float dm_step, uint32_t dm,
+                           float shift) {
+  volatile float step_dm = static_cast<float>(dm) * dm_step;
+  volatile float dm_value = first_dm + step_dm;
+  volatile float product = dm_value * shift;
+  return static_cast<uint32_t>(product);
+}
+
+}  // namespace dd

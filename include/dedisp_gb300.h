@@ -1,0 +1,251 @@
+/*
+ * dedisp_gb300.h -- C ABI of the GB300 incoherent dedispersion engine.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, never
+ * throws, and returns a dd_status (0 = success, negative = error).  The text
+ * of the most recent error on the calling thread is returned by
+ * dd_last_error().  There is no CPU fallback: without a CUDA device every
+ * compute entry point returns DD_ERR_NO_DEVICE.
+ *
+ * The algorithm is the direct-sum (brute force) dedispersion of
+ * TRASAL/Dedispersion:
+ *
+ *   out[g][dm][t] = sum over live channels c of g of
+ *                   in[row(g, c)][t + (uint)((firstDM + dm * dmStep) * shift[c])]
+ *
+ * in single-step form (include/Dedispersion.hpp:70-109 of the reference) and
+ * in two-step subband form (include/Dedispersion.hpp:111-176).  Data layouts
+ * are the reference's: rows padded to `padding` bytes (isa::utils::pad), the
+ * output [synthesized beam][DM][padded samples] in float32.
+ *
+ * Input sample types are chosen by `input_bits`:
+ *   1, 2, 4  packed little-endian within bytes (sample k of a row lives in
+ *            byte k / (8 / bits) at bit (k % (8 / bits)) * bits), unsigned,
+ *   8        uint8_t,
+ *   16       uint16_t,
+ *   32       float.
+ * Integer inputs are accumulated exactly in 32-bit integers and converted to
+ * float once; float input is accumulated in float32 in channel order, which
+ * is the reference's own order, so results equal the reference's bit for bit.
+ */
+#ifndef DEDISP_GB300_H
+#define DEDISP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DD_ABI_VERSION 1
+
+typedef enum dd_status {
+  DD_OK = 0,
+  DD_ERR_INVALID_ARGUMENT = -1, /* bad shape, null pointer, bad enum */
+  DD_ERR_NO_DEVICE = -2,        /* no CUDA device visible */
+  DD_ERR_CUDA = -3,             /* a CUDA runtime call failed */
+  DD_ERR_OUT_OF_MEMORY = -4,    /* device allocation failed */
+  DD_ERR_UNSUPPORTED = -5,      /* input bits / tile config not supported */
+  DD_ERR_TIMEOUT = -6,          /* a bounded device-side wait ran out */
+  DD_ERR_FILE = -7,             /* a file could not be opened or parsed */
+  DD_ERR_OVER_BUDGET = -8,      /* a request exceeds the memory budget */
+  DD_ERR_NOT_FOUND = -9         /* a lookup found nothing */
+} dd_status;
+
+typedef enum dd_mode {
+  DD_SINGLE_STEP = 0, /* Dedispersion::dedispersion */
+  DD_STEP_ONE = 1,    /* Dedispersion::subbandDedispersionStepOne */
+  DD_STEP_TWO = 2     /* Dedispersion::subbandDedispersionStepTwo */
+} dd_mode;
+
+/*
+ * Geometry of one observation batch.  Field-for-field the state the
+ * reference reads through AstroData::Observation (getters listed at
+ * include/Dedispersion.hpp:70-176 and src/Shifts.cpp:20-42).  Fields with a
+ * `_subbanding` suffix are the values the reference reads with
+ * `subbanding = true`.
+ */
+typedef struct dd_observation {
+  uint32_t nr_beams;
+  uint32_t nr_synthesized_beams;
+  uint32_t nr_channels;
+  uint32_t nr_subbands;                     /* 1 in single-step mode */
+  uint32_t nr_samples_per_batch;            /* S  */
+  uint32_t nr_samples_per_dispersed_batch;  /* S_disp >= S + max delay */
+  uint32_t nr_samples_per_batch_subbanding; /* S1 (step one output length) */
+  uint32_t nr_samples_per_dispersed_batch_subbanding; /* S1_disp */
+  uint32_t nr_dms;
+  uint32_t nr_dms_subbanding;
+  uint32_t downsampling;                    /* must be 1 (AstroData default) */
+  uint32_t nr_zapped_channels;              /* informational */
+  float first_dm;
+  float dm_step;
+  float first_dm_subbanding;
+  float dm_step_subbanding;
+  float sampling_time;                      /* seconds */
+  float min_freq;                           /* MHz, lowest channel */
+  float channel_bandwidth;                  /* MHz */
+} dd_observation;
+
+/*
+ * Tile configuration; field-for-field Dedispersion::DedispersionConf
+ * (include/Dedispersion.hpp:34-54) plus the isa::OpenCL::KernelConf
+ * threads/items it extends.  Meaning on the GPU:
+ *   threads_d0  threads along time (32: one warp spans the time axis)
+ *   threads_d1  warps along the DM axis
+ *   items_d0    samples per thread (a multiple of 4)
+ *   items_d1    DMs per thread
+ *   unroll      channels staged per pipeline stage
+ *   local_mem   1 = rows staged to shared memory by bulk copies (TMA)
+ *   split_batches  kept for the tuned-file format; must be 0
+ */
+typedef struct dd_conf {
+  uint32_t split_batches;
+  uint32_t local_mem;
+  uint32_t unroll;
+  uint32_t threads_d0;
+  uint32_t threads_d1;
+  uint32_t threads_d2;
+  uint32_t items_d0;
+  uint32_t items_d1;
+  uint32_t items_d2;
+} dd_conf;
+
+/* Row pitches and buffer sizes the reference's layout gives for one mode. */
+typedef struct dd_layout {
+  uint64_t input_row_bytes;   /* bytes between consecutive channel rows */
+  uint64_t input_bytes;       /* whole input buffer */
+  uint64_t output_row_elems;  /* floats between consecutive DM rows */
+  uint64_t output_bytes;      /* whole output buffer */
+  uint64_t mapping_row_elems; /* uint32 per synthesized beam in beamMapping */
+  uint64_t zapped_elems;      /* uint32 entries of the zapped mask */
+  uint64_t shifts_elems;      /* floats of the shift table */
+  uint32_t max_delay;         /* largest per-channel delay in samples */
+  uint32_t required_dispersed_samples; /* S (or S1) + max_delay */
+} dd_layout;
+
+/* ---- library ------------------------------------------------------------ */
+
+/* Message of the last error raised on this thread ("" if none). */
+const char *dd_last_error(void);
+/* DD_ABI_VERSION of the loaded library. */
+int dd_version(void);
+/* Number of visible CUDA devices (0 on a host without a GPU). */
+dd_status dd_device_count(int *count);
+
+/* ---- host geometry (no device needed) ----------------------------------- */
+
+/* isa::utils::pad: round `value` up to a multiple of `padding` (0 = none). */
+uint64_t dd_pad(uint64_t value, uint64_t padding);
+
+/* Dedispersion::getShifts (src/Shifts.cpp:20-30): per-channel delay in
+ * samples per unit DM; the table is pad(C, padding/4) floats, last channel
+ * and padding zero.  `capacity` is the number of floats `shifts` holds. */
+dd_status dd_get_shifts(const dd_observation *obs, uint32_t padding,
+                        float *shifts, size_t capacity);
+
+/* Dedispersion::getShiftsStepTwo (src/Shifts.cpp:32-42): per-subband delay
+ * per unit DM, relative to the highest channel of each subband. */
+dd_status dd_get_shifts_step_two(const dd_observation *obs, uint32_t padding,
+                                 float *shifts, size_t capacity);
+
+/* Observation frequency getters (AstroData::Observation). */
+float dd_max_freq(const dd_observation *obs);
+float dd_subband_min_freq(const dd_observation *obs);
+float dd_subband_max_freq(const dd_observation *obs);
+float dd_subband_bandwidth(const dd_observation *obs);
+
+/* Buffer layout of one mode.  `shifts` may be NULL (max_delay is then 0). */
+dd_status dd_get_layout(const dd_observation *obs, dd_mode mode,
+                        uint32_t input_bits, uint32_t padding,
+                        const float *shifts, dd_layout *layout);
+
+/* Default tile configuration the engine picks for a mode and input type. */
+dd_status dd_default_conf(const dd_observation *obs, dd_mode mode,
+                          uint32_t input_bits, dd_conf *conf);
+
+/* DedispersionConf::print (src/Dedispersion.cpp:87-89):
+ * "split local unroll tD0 tD1 tD2 iD0 iD1 iD2".  Writes at most `capacity`
+ * bytes including the terminating NUL. */
+dd_status dd_conf_print(const dd_conf *conf, char *text, size_t capacity);
+
+/* readTunedDedispersionConf (src/Dedispersion.cpp:20-81): look up the entry
+ * for (`device`, `nr_dms`) in a tuned-configuration text file whose lines
+ * read "device nrDMs split local unroll tD0 tD1 tD2 iD0 iD1 iD2"; lines not
+ * starting with a letter are ignored.  DD_ERR_FILE if the file cannot be
+ * opened, DD_ERR_NOT_FOUND if no line matches. */
+dd_status dd_read_tuned_conf(const char *path, const char *device,
+                             uint32_t nr_dms, dd_conf *conf);
+
+/* Append one line in the same format to `path`. */
+dd_status dd_write_tuned_conf(const char *path, const char *device,
+                              uint32_t nr_dms, const dd_conf *conf);
+
+/* ---- synchronous host-buffer calls -------------------------------------- */
+/* Drop-in replacements of the reference's CPU templates.  Host pointers in
+ * the reference layout; the call copies to the device, runs, copies the
+ * result back and returns when `output` holds it. */
+
+/* Dedispersion::dedispersion<I,L,O> (include/Dedispersion.hpp:59, 70-109). */
+dd_status dd_dedispersion(const dd_observation *obs, const uint32_t *zapped,
+                          const uint32_t *beam_mapping, const void *input,
+                          float *output, const float *shifts,
+                          uint32_t padding, uint32_t input_bits);
+
+/* Dedispersion::subbandDedispersionStepOne (include/Dedispersion.hpp:60,
+ * 111-153).  Output layout [beam][DM1][subband][pad(S1)]. */
+dd_status dd_subband_dedispersion_step_one(const dd_observation *obs,
+                                           const uint32_t *zapped,
+                                           const void *input, float *output,
+                                           const float *shifts,
+                                           uint32_t padding,
+                                           uint32_t input_bits);
+
+/* Dedispersion::subbandDedispersionStepTwo (include/Dedispersion.hpp:61,
+ * 155-176).  Float input [beam][DM1][subband][pad(S1)], output
+ * [synthesized beam][DM1 * DM2][pad(S)]. */
+dd_status dd_subband_dedispersion_step_two(const dd_observation *obs,
+                                           const uint32_t *beam_mapping,
+                                           const float *input, float *output,
+                                           const float *shifts,
+                                           uint32_t padding);
+
+/* ---- plans: device-resident tables, asynchronous device-pointer runs ---- */
+/* The device twins of the generated OpenCL kernels `dedispersion`,
+ * `dedispersionStepOne`, `dedispersionStepTwo` (include/Dedispersion.hpp:
+ * 203-540, 543-882, 884-1122), launched as src/DedispersionTest.cpp:366-399
+ * launches them.  A plan owns its device tables; the caller owns the data
+ * buffers.  A plan is used from one thread/stream at a time; distinct plans
+ * are independent. */
+typedef struct dd_plan dd_plan;
+
+/* `conf` may be NULL (dd_default_conf).  `device` is a CUDA device index. */
+dd_status dd_plan_create(dd_plan **plan, const dd_observation *obs,
+                         dd_mode mode, uint32_t input_bits, uint32_t padding,
+                         const dd_conf *conf, int device);
+/* Host tables, copied to the device.  Shifts are required; the zapped mask
+ * (nonzero = skip) defaults to none zapped, the beam mapping to identity. */
+dd_status dd_plan_set_shifts(dd_plan *plan, const float *shifts, size_t n);
+dd_status dd_plan_set_zapped(dd_plan *plan, const uint32_t *zapped, size_t n);
+dd_status dd_plan_set_beam_mapping(dd_plan *plan, const uint32_t *mapping,
+                                   size_t n);
+/* Enqueue one run on `stream` (a cudaStream_t; NULL = legacy default).
+ * Device pointers in the layout dd_get_layout describes; returns after the
+ * launch is queued. */
+dd_status dd_plan_run(dd_plan *plan, const void *d_input, float *d_output,
+                      void *stream);
+/* Synchronize `stream` and report any device-side error the plan recorded
+ * (DD_ERR_TIMEOUT for an expired bounded wait). */
+dd_status dd_plan_check(dd_plan *plan, void *stream);
+/* Kernel launches one dd_plan_run enqueues. */
+dd_status dd_plan_launches(const dd_plan *plan, uint32_t *launches);
+/* The configuration the plan runs with. */
+dd_status dd_plan_get_conf(const dd_plan *plan, dd_conf *conf);
+dd_status dd_plan_destroy(dd_plan *plan);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* DEDISP_GB300_H */
