@@ -1,0 +1,328 @@
+"""Throughput benchmark of the dedispersion engine on the 1536-channel,
+2048-DM, 24576-sample 8-bit workload (single step, bit-exact integer sums).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  Metric: DM-samples/s = DM trials x output
+samples per second.
+
+* value      -- device-resident: K back-to-back runs of the plain kernel on
+                inputs already in HBM, timed with CUDA events on the launching
+                stream.  Inputs rotate over 4 buffers (4 x 45 MB) while every
+                step also writes its 201 MB output, so each step starts with its
+                input out of L2.
+* e2e        -- the same metric through the C ABI's synchronous host-buffer
+                call dd_dedispersion (the reference's drop-in): pinned host
+                input copied to the device, kernel, output copied back, all
+                inside the timed region.
+* roofline   -- the kernel is add-bound (1459 live channels: 1459 adds per
+                DM-sample against 4.9 compulsory bytes); achieved adds/s over
+                the scalar add rate of 152 SMs x 128 lanes at the SM clock
+                sampled during the run, plus the HBM view of the same launch.
+* cpu_baseline -- the CPU oracle (a loop-for-loop port of the reference's
+                dedispersion) on all host cores over a DM prefix of the same
+                workload.
+
+With --impl reference the CPU port alone is timed, each step a DM prefix of
+the workload, on all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "DM-samples/s (DM trials x output samples per second), 1536ch x 2048DM x 24576 8-bit, bit-exact"
+UNIT = "DM-samples/s"
+WORKLOAD = "single-step 1536ch x 2048DM x 24576 samples, uint8 N(128,20) + 20 pulses, 5% zapped"
+PADDING = 128
+SMS = 152
+LANES = 128
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=2.0,
+                    help="target wall time of the CPU baseline sample")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(seed=1):
+    import dedispersion_gb300 as dd
+    from dedispersion_gb300 import synthetic as syn
+    obs = syn.large_observation(PADDING)
+    shifts = dd.getShifts(obs, PADDING)
+    zapped = syn.zapped_mask(1536, 0.05, 7, PADDING)
+    mapping = syn.identity_mapping(obs, PADDING)
+    inp = syn.make_input(obs, 8, PADDING, seed=seed, mean=128.0, sigma=20.0, pulses=20,
+                         shifts=shifts)
+    return obs, shifts, zapped, mapping, inp
+
+
+class ClockSampler:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
+                    rows.append(parts)
+        finally:
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": float(rows[0][2]),
+                "reasons": reasons, "samples": len(rows),
+                "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())}
+
+
+def read_profile_traffic():
+    """DRAM bytes per launch of the plain kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "swar8_plain_1536ch_2048dm_8bit.md"
+    if not p.exists():
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9]+)", p.read_text())
+    return int(m.group(1)) if m else None
+
+
+def cpu_sample(obs, shifts, zapped, mapping, inp, target_s, threads):
+    """Time the oracle on a DM prefix sized for ~target_s of wall time;
+    returns (DM-samples/s, dms, seconds)."""
+    import oracle
+    out = np.zeros(obs.getNrDMs() * dd_out_row(obs), dtype=np.float32)
+    dms = 2
+    while True:
+        t = time.perf_counter()
+        oracle.dedispersion(obs.c, zapped, mapping, inp, out, shifts, PADDING, 8, 0, dms, threads)
+        dt = time.perf_counter() - t
+        if dt >= target_s * 0.5 or dms >= obs.getNrDMs():
+            return dms * obs.getNrSamplesPerBatch() / dt, dms, dt
+        dms = min(obs.getNrDMs(), max(dms + 1, int(dms * target_s / max(dt, 1e-3))))
+
+
+def dd_out_row(obs):
+    import dedispersion_gb300 as dd
+    return dd.pad(obs.getNrSamplesPerBatch(), PADDING // 4)
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    obs, shifts, zapped, mapping, inp = workload()
+    threads = os.cpu_count() or 1
+    import oracle
+    out = np.zeros(obs.getNrDMs() * dd_out_row(obs), dtype=np.float32)
+    # size one step's DM prefix for ~1/(steps+warmup) of a ~60 s budget
+    _, dms, dt = cpu_sample(obs, shifts, zapped, mapping, inp,
+                            max(0.5, 60.0 / (args.steps + args.warmup)), threads)
+    for _ in range(args.warmup):
+        oracle.dedispersion(obs.c, zapped, mapping, inp, out, shifts, PADDING, 8, 0, dms, threads)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.dedispersion(obs.c, zapped, mapping, inp, out, shifts, PADDING, 8, 0, dms, threads)
+    elapsed = time.perf_counter() - t
+    value = args.steps * dms * obs.getNrSamplesPerBatch() / elapsed
+    sample = (f"DMs 0..{dms - 1} of 2048 x 24576 samples x 1536 channels per step "
+              f"(same delays as the full workload)")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+        "data": "synthetic", "config": {"workload": WORKLOAD, "dm_prefix": dms},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if world > 1 and args.impl == "reference" and rank != 0:
+        return
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    import dedispersion_gb300 as dd
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        pg = tdist
+
+    obs, shifts, zapped, mapping, inp = workload(seed=1 + rank)
+    S, D = obs.getNrSamplesPerBatch(), obs.getNrDMs()
+    live = int((zapped[:1536] == 0).sum())
+    lay = dd.layout(obs, dd.DD_SINGLE_STEP, 8, PADDING, shifts)
+    plan = dd.Plan(obs, dd.DD_SINGLE_STEP, 8, PADDING, device=local)
+    plan.setShifts(shifts)
+    plan.setZappedChannels(zapped)
+    plan.setBeamMapping(mapping)
+    nbuf = 4
+    d_in = [torch.from_numpy(inp).to(f"cuda:{local}") for _ in range(nbuf)]
+    d_out = torch.empty(lay.output_bytes // 4, dtype=torch.float32, device=f"cuda:{local}")
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+        torch.cuda.synchronize()
+
+    for i in range(args.warmup):
+        plan.run(d_in[i % nbuf], d_out, stream)
+    plan.check(stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for i in range(args.steps):
+            plan.run(d_in[i % nbuf], d_out, stream)
+        e1.record(stream)
+        barrier()
+        # keep the GPU busy for the clock sampler if the timed region was short
+        ms = e0.elapsed_time(e1)
+    plan.check(stream)
+    clocks = clk.summary()
+    t_dev = ms / 1e3
+    if pg is not None:
+        t = torch.tensor([t_dev], device=f"cuda:{local}")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        t_dev = float(t.item())
+    units = world * args.steps * D * S
+    value = units / t_dev
+    per_launch_s = t_dev / args.steps
+
+    # e2e through the C ABI's synchronous host-buffer call, pinned host memory
+    h_in = torch.from_numpy(inp).pin_memory()
+    h_out = torch.empty(lay.output_bytes // 4, dtype=torch.float32).pin_memory()
+    in_np, out_np = h_in.numpy(), h_out.numpy()
+    e2e_steps = max(3, min(args.steps, 10))
+    for _ in range(2):
+        dd.dedispersion(obs, zapped, mapping, in_np, out_np, shifts, PADDING, 8)
+    barrier()
+    t = time.perf_counter()
+    for _ in range(e2e_steps):
+        dd.dedispersion(obs, zapped, mapping, in_np, out_np, shifts, PADDING, 8)
+    barrier()
+    t_e2e = time.perf_counter() - t
+    if pg is not None:
+        tt = torch.tensor([t_e2e], device=f"cuda:{local}")
+        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    e2e_value = world * e2e_steps * D * S / t_e2e
+
+    if rank != 0:
+        return
+    # roofline of the plain kernel
+    adds_per_launch = D * S * live
+    achieved_adds = adds_per_launch / per_launch_s
+    sm_mhz = clocks.get("sm_mhz") or 2070.0
+    peak_adds = SMS * LANES * sm_mhz * 1e6
+    compulsory = inp.nbytes // 1 + D * S * 4
+    hbm_peak = 6784.2
+    try:
+        hbm_peak = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"]
+    except Exception:
+        pass
+    traffic = read_profile_traffic()
+    cpu_threads = os.cpu_count() or 1
+    cpu_val, cpu_dms, cpu_dt = cpu_sample(obs, shifts, zapped, mapping, inp, args.cpu_seconds,
+                                          cpu_threads)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "padding": PADDING, "live_channels": live,
+                   "kernel_conf": plan.conf().print(),
+                   "l2": "inputs rotate over 4 device buffers (4 x 45 MB) and each step writes "
+                         "201 MB of output, so every step reads its input from HBM",
+                   "parallelism": f"{world} independent beams (one per GPU)"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(inp.nbytes),
+                "d2h_bytes_per_step": int(D * S * 4),
+                "call": "dd_dedispersion (C ABI, synchronous, host buffers)"},
+        "roofline": {"bound": "alu", "achieved": achieved_adds / 1e9, "peak": peak_adds / 1e9,
+                     "unit": "Gadd/s", "frac": achieved_adds / peak_adds,
+                     "traffic": traffic,
+                     "peak_source": f"scalar add issue rate: {SMS} SMs x {LANES} lanes x "
+                                    f"{sm_mhz:.0f} MHz (median SM clock sampled during the run)",
+                     "adds_per_launch": adds_per_launch,
+                     "hbm": {"achieved_gbs": compulsory / per_launch_s / 1e9,
+                             "peak_gbs": hbm_peak,
+                             "frac": compulsory / per_launch_s / 1e9 / hbm_peak,
+                             "compulsory_bytes_per_launch": compulsory}},
+        "cpu_baseline": {"value": cpu_val, "unit": UNIT, "cores": cpu_threads, "kind": "port",
+                         "sample": f"DMs 0..{cpu_dms - 1} of 2048 (all 24576 samples, 1536 "
+                                   f"channels), {cpu_dt:.2f} s wall on {cpu_threads} threads"},
+        "clocks": clocks,
+        "gpu_launches": args.steps * plan.launches(),
+    }
+    print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -335,6 +335,28 @@ def writeTunedDedispersionConf(filename: str, device: str, nrDMs: int,
     check(lib().dd_write_tuned_conf(filename.encode(), device.encode(), nrDMs, C.byref(c)))
 
 
+@dataclass
+class KernelEntry:
+    """One compiled tile configuration of the engine."""
+
+    index: int
+    name: str
+    elem_bits: int
+    conf: DedispersionConf
+
+
+def kernels() -> list[KernelEntry]:
+    """Every compiled tile configuration (the tuner's search space)."""
+    out = []
+    for i in range(lib().dd_kernel_count()):
+        name = C.create_string_buffer(128)
+        bits = C.c_uint32(0)
+        c = DdConf()
+        check(lib().dd_kernel_info(i, name, 128, C.byref(bits), C.byref(c)))
+        out.append(KernelEntry(i, name.value.decode(), bits.value, DedispersionConf.from_c(c)))
+    return out
+
+
 def _devptr(x) -> int:
     if x is None:
         return 0
@@ -358,13 +380,19 @@ class Plan:
     stream with device pointers (raw ints or tensors exposing data_ptr())."""
 
     def __init__(self, observation: Observation, mode: int, inputBits: int, padding: int,
-                 conf: DedispersionConf | None = None, device: int = 0):
+                 conf: DedispersionConf | None = None, device: int = 0,
+                 kernel: int | None = None):
         self.observation = observation.copy()
         self.mode, self.inputBits, self.padding = mode, inputBits, padding
         self._h = C.c_void_p()
-        cc = conf.to_c() if conf is not None else None
-        check(lib().dd_plan_create(C.byref(self._h), C.byref(self.observation.c), mode, inputBits,
-                                   padding, C.byref(cc) if cc is not None else None, device))
+        if kernel is not None:
+            check(lib().dd_plan_create_with_kernel(C.byref(self._h), C.byref(self.observation.c),
+                                                   mode, inputBits, padding, kernel, device))
+        else:
+            cc = conf.to_c() if conf is not None else None
+            check(lib().dd_plan_create(C.byref(self._h), C.byref(self.observation.c), mode,
+                                       inputBits, padding,
+                                       C.byref(cc) if cc is not None else None, device))
         self.layout = layout(self.observation, mode, inputBits if mode != DD_STEP_TWO else 32,
                              padding)
 

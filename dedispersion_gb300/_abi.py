@@ -110,6 +110,10 @@ SIGNATURES = {
                                                    C.c_uint32]),
     "dd_plan_create": (C.c_int, [C.POINTER(_P), _OBS, C.c_int, C.c_uint32, C.c_uint32,
                                  _CONF, C.c_int]),
+    "dd_kernel_count": (C.c_int, []),
+    "dd_kernel_info": (C.c_int, [C.c_int, C.c_char_p, C.c_size_t, _U32P, _CONF]),
+    "dd_plan_create_with_kernel": (C.c_int, [C.POINTER(_P), _OBS, C.c_int, C.c_uint32,
+                                             C.c_uint32, C.c_int, C.c_int]),
     "dd_plan_set_shifts": (C.c_int, [_P, _F32P, C.c_size_t]),
     "dd_plan_set_zapped": (C.c_int, [_P, _U32P, C.c_size_t]),
     "dd_plan_set_beam_mapping": (C.c_int, [_P, _U32P, C.c_size_t]),

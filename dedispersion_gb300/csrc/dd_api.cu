@@ -580,6 +580,45 @@ dd_status dd_plan_create(dd_plan **plan, const dd_observation *o, dd_mode mode,
   return DD_OK;
 }
 
+int dd_kernel_count(void) {
+  int n = 0;
+  dd::kernel_registry(&n);
+  return n;
+}
+
+dd_status dd_kernel_info(int index, char *name, size_t capacity, uint32_t *elem_bits,
+                         dd_conf *conf) {
+  int n = 0;
+  const dd::KernelInfo *reg = dd::kernel_registry(&n);
+  if (index < 0 || index >= n) return fail(DD_ERR_INVALID_ARGUMENT, "kernel index %d out of range", index);
+  if (name && capacity) {
+    std::strncpy(name, reg[index].name, capacity);
+    name[capacity - 1] = 0;
+  }
+  if (elem_bits) *elem_bits = (uint32_t)reg[index].elem_bits;
+  if (conf) *conf = conf_of(reg[index]);
+  return DD_OK;
+}
+
+dd_status dd_plan_create_with_kernel(dd_plan **plan, const dd_observation *o, dd_mode mode,
+                                     uint32_t input_bits, uint32_t padding, int kernel_index,
+                                     int device) {
+  int n = 0;
+  const dd::KernelInfo *reg = dd::kernel_registry(&n);
+  if (kernel_index < 0 || kernel_index >= n)
+    return fail(DD_ERR_INVALID_ARGUMENT, "kernel index %d out of range", kernel_index);
+  const uint32_t bits = mode == DD_STEP_TWO ? 32 : input_bits;
+  if (!bits_ok(bits)) return fail(DD_ERR_UNSUPPORTED, "input_bits %u not supported", bits);
+  if ((uint32_t)reg[kernel_index].elem_bits != family_bits(mode, bits))
+    return fail(DD_ERR_UNSUPPORTED, "kernel %s does not take %u-bit input", reg[kernel_index].name,
+                bits);
+  dd_conf c = conf_of(reg[kernel_index]);
+  dd_status st = dd_plan_create(plan, o, mode, input_bits, padding, &c, device);
+  if (st) return st;
+  (*plan)->kinfo = &reg[kernel_index];
+  return DD_OK;
+}
+
 dd_status dd_plan_set_shifts(dd_plan *p, const float *shifts, size_t n) {
   if (!p || !shifts) return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
   size_t need = p->mode == DD_STEP_TWO ? p->obs.nr_subbands : p->obs.nr_channels;
@@ -637,6 +676,7 @@ dd_status dd_plan_run(dd_plan *p, const void *d_input, float *d_output, void *st
   P.tiles_d = p->tiles_d;
   P.tma = (d.row_bytes % 16 == 0 && reinterpret_cast<uintptr_t>(d_input) % 16 == 0) ? 1u : 0u;
   P.out_vec4 = (d.out_row % 4 == 0 && reinterpret_cast<uintptr_t>(d_output) % 16 == 0) ? 1u : 0u;
+  P.mul_hi8 = 1u << 24;
   DeviceGuard g(p->device);
   if (!g.ok) return fail(DD_ERR_CUDA, "cannot select device %d", p->device);
   p->kinfo->launch(P, (unsigned)tiles, p->smem, static_cast<cudaStream_t>(stream));

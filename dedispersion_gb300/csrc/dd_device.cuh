@@ -251,9 +251,27 @@ __device__ __forceinline__ void drain_stages(const StageCtx &S, uint32_t sc,
 
 // ---- swar8 tile -----------------------------------------------------------
 
+// Inner-loop variants of the swar8 family.  Both keep sums exact.
+//
+// kUnpackPermute: two byte permutes spread a word's samples (b0 b1 b2 b3)
+//   into two registers of 16-bit lanes, (b0, b1) and (b2, b3), and integer
+//   adds accumulate them (all on the integer ALU pipe).
+// kUnpackMaskHigh: one AND keeps the even samples, E += w & 0x00FF00FF
+//   (lanes b0, b2), and one high-half multiply-add on the FMA pipe adds
+//   w >> 8 = b1 + 2^8 b2 + 2^16 b3 to a plain 32-bit sum A.  After at most
+//   256 rows A = S1 + 2^8 S2 + 2^16 S3 < 2^32 exactly; S2 is E's high lane, so
+//   A - (S2 << 8) = S1 + 2^16 S3 with S1 < 2^16 splits into S1 and S3.
+enum { kUnpackPermute = 0, kUnpackMaskHigh = 1 };
+
+__device__ __forceinline__ uint32_t mad_hi(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t d;
+  asm("mad.hi.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+  return d;
+}
+
 // Computes one tile; returns false if the CTA must stop (timeout).  `sc`
 // counts the CTA's stages across tiles (mbarrier phase bookkeeping).
-template <int NW, int NDT, int TY, int CH>
+template <int NW, int NDT, int TY, int CH, int VAR>
 __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
                                            const GroupDesc &G, uint32_t dtile,
                                            uint32_t ttile, uint8_t *smem,
@@ -267,6 +285,7 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
   const uint32_t K = G.entry_count;
   const uint32_t nst = (K + CH - 1) / CH;
   const uint32_t cw = L.copy_words;
+  const uint32_t mul = P.mul_hi8;
   StageCtx S;
   S.bars = reinterpret_cast<uint64_t *>(smem + L.off_bar);
   S.wstart = reinterpret_cast<uint32_t *>(smem + L.off_wstart);
@@ -281,6 +300,8 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
       issue_stage<CH>(P, G, S, s, sc + s, t0, d0, tx);
   }
 
+  // kUnpackPermute: lo = (b0, b1) lanes, hi = (b2, b3) lanes.
+  // kUnpackMaskHigh: lo = E (b0, b2 lanes), hi = A (w >> 8 sum).
   uint32_t lo[NDT][NW], hi[NDT][NW], tot[NDT][NW][4];
 #pragma unroll
   for (int j = 0; j < NDT; ++j)
@@ -290,6 +311,28 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
       tot[j][i][0] = tot[j][i][1] = tot[j][i][2] = tot[j][i][3] = 0;
     }
   uint32_t since = 0;
+
+  auto flush = [&]() {
+#pragma unroll
+    for (int j = 0; j < NDT; ++j)
+#pragma unroll
+      for (int i = 0; i < NW; ++i) {
+        if (VAR == kUnpackPermute) {
+          tot[j][i][0] += lo[j][i] & 0xFFFFu;
+          tot[j][i][1] += lo[j][i] >> 16;
+          tot[j][i][2] += hi[j][i] & 0xFFFFu;
+          tot[j][i][3] += hi[j][i] >> 16;
+        } else {
+          const uint32_t s2 = lo[j][i] >> 16;
+          const uint32_t x = hi[j][i] - (s2 << 8);
+          tot[j][i][0] += lo[j][i] & 0xFFFFu;
+          tot[j][i][1] += x & 0xFFFFu;
+          tot[j][i][2] += s2;
+          tot[j][i][3] += x >> 16;
+        }
+        lo[j][i] = hi[j][i] = 0;
+      }
+  };
 
   for (uint32_t s = 0; s < nst; ++s) {
     const uint32_t gs = sc + s, slot = gs % kNRaw, area = gs & 1u;
@@ -339,53 +382,56 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
       issue_stage<CH>(P, G, S, s + kNRaw, gs + kNRaw, t0, d0, tx);
 
     if (since + cnt > 256u) {
-#pragma unroll
-      for (int j = 0; j < NDT; ++j)
-#pragma unroll
-        for (int i = 0; i < NW; ++i) {
-          tot[j][i][0] += lo[j][i] & 0xFFFFu;
-          tot[j][i][1] += lo[j][i] >> 16;
-          tot[j][i][2] += hi[j][i] & 0xFFFFu;
-          tot[j][i][3] += hi[j][i] >> 16;
-          lo[j][i] = hi[j][i] = 0;
-        }
+      flush();
       since = 0;
     }
     since += cnt;
 
     const uint32_t *tbt = tb + ty * NDT;
+    const uint32_t *act = ac + tx;
     uint32_t ch = 0;
     for (; ch + 1 < cnt; ch += 2) {
-      uint32_t b1[NDT], b2[NDT];
+      const uint32_t *p1[NDT], *p2[NDT];
 #pragma unroll
       for (int j = 0; j < NDT; ++j) {
-        b1[j] = tbt[ch * kTileD + j] + tx;
-        b2[j] = tbt[(ch + 1) * kTileD + j] + tx;
+        p1[j] = act + tbt[ch * kTileD + j];
+        p2[j] = act + tbt[(ch + 1) * kTileD + j];
       }
 #pragma unroll
       for (int j = 0; j < NDT; ++j)
 #pragma unroll
         for (int i = 0; i < NW; ++i) {
-          const uint32_t w1 = ac[b1[j] + 32 * i];
-          const uint32_t w2 = ac[b2[j] + 32 * i];
-          lo[j][i] += __byte_perm(w1, 0, 0x4140) + __byte_perm(w2, 0, 0x4140);
-          hi[j][i] += __byte_perm(w1, 0, 0x4342) + __byte_perm(w2, 0, 0x4342);
+          const uint32_t w1 = p1[j][32 * i];
+          const uint32_t w2 = p2[j][32 * i];
+          if (VAR == kUnpackPermute) {
+            lo[j][i] += __byte_perm(w1, 0, 0x4140) + __byte_perm(w2, 0, 0x4140);
+            hi[j][i] += __byte_perm(w1, 0, 0x4342) + __byte_perm(w2, 0, 0x4342);
+          } else {
+            lo[j][i] += (w1 & 0x00FF00FFu) + (w2 & 0x00FF00FFu);
+            hi[j][i] = mad_hi(w2, mul, mad_hi(w1, mul, hi[j][i]));
+          }
         }
     }
     if (ch < cnt) {
 #pragma unroll
       for (int j = 0; j < NDT; ++j) {
-        const uint32_t b = tbt[ch * kTileD + j] + tx;
+        const uint32_t *p = act + tbt[ch * kTileD + j];
 #pragma unroll
         for (int i = 0; i < NW; ++i) {
-          const uint32_t w = ac[b + 32 * i];
-          lo[j][i] += __byte_perm(w, 0, 0x4140);
-          hi[j][i] += __byte_perm(w, 0, 0x4342);
+          const uint32_t w = p[32 * i];
+          if (VAR == kUnpackPermute) {
+            lo[j][i] += __byte_perm(w, 0, 0x4140);
+            hi[j][i] += __byte_perm(w, 0, 0x4342);
+          } else {
+            lo[j][i] += w & 0x00FF00FFu;
+            hi[j][i] = mad_hi(w, mul, hi[j][i]);
+          }
         }
       }
     }
   }
   sc += nst;
+  flush();
 
 #pragma unroll
   for (int j = 0; j < NDT; ++j) {
@@ -394,10 +440,8 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
     float *orow = P.out + G.out_offset + (uint64_t)d * P.out_dm_stride;
 #pragma unroll
     for (int i = 0; i < NW; ++i) {
-      const uint32_t v0 = tot[j][i][0] + (lo[j][i] & 0xFFFFu);
-      const uint32_t v1 = tot[j][i][1] + (lo[j][i] >> 16);
-      const uint32_t v2 = tot[j][i][2] + (hi[j][i] & 0xFFFFu);
-      const uint32_t v3 = tot[j][i][3] + (hi[j][i] >> 16);
+      const uint32_t v0 = tot[j][i][0], v1 = tot[j][i][1];
+      const uint32_t v2 = tot[j][i][2], v3 = tot[j][i][3];
       const uint32_t t = t0 + 4u * (tx + 32u * i);
       if (P.out_vec4 && t + 3u < P.nr_samples) {
         *reinterpret_cast<float4 *>(orow + t) =

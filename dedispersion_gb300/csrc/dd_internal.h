@@ -62,7 +62,7 @@ struct ProblemDesc {
   uint32_t tiles_d;        // DM tiles per group
   uint32_t tma;            // 1: rows staged by bulk async copies
   uint32_t out_vec4;       // 1: float4 stores are aligned
-  uint32_t reserved;
+  uint32_t mul_hi8;        // always 1 << 24 (w >> 8 as a high-half multiply)
 };
 
 // One entry of the kernel registry: a compiled tile configuration.
@@ -77,6 +77,7 @@ struct KernelInfo {
   int threads;
   int tile_t;       // samples per tile
   int tile_d;       // DMs per tile
+  int variant;      // swar8 inner loop (kUnpackMaskHigh / kUnpackPermute)
   const void *func;
   void (*launch)(const ProblemDesc &, unsigned grid, size_t smem,
                  cudaStream_t stream);

@@ -13,7 +13,7 @@
 namespace dd {
 
 // Grid-mapped kernel: one CTA per tile.
-template <int NW, int NDT, int TY, int CH>
+template <int NW, int NDT, int TY, int CH, int VAR>
 __global__ void __launch_bounds__(32 * TY, (TY >= 8 ? 2 : 4))
     swar8_kernel(const ProblemDesc P) {
   extern __shared__ __align__(128) uint8_t smem[];
@@ -21,7 +21,7 @@ __global__ void __launch_bounds__(32 * TY, (TY >= 8 ? 2 : 4))
   init_barriers(smem, L, CH);
   uint32_t g, dtile, ttile, sc = 0;
   decode_tile(P, blockIdx.x, g, dtile, ttile);
-  (void)swar8_tile<NW, NDT, TY, CH>(P, P.groups[g], dtile, ttile, smem, L, sc);
+  (void)swar8_tile<NW, NDT, TY, CH, VAR>(P, P.groups[g], dtile, ttile, smem, L, sc);
 }
 
 template <typename T, int NS, int NDT, int TY, int CH>
@@ -35,10 +35,10 @@ __global__ void __launch_bounds__(32 * TY, (TY >= 8 ? 2 : 4))
   (void)scalar_tile<T, NS, NDT, TY, CH>(P, P.groups[g], dtile, ttile, smem, L, sc);
 }
 
-template <int NW, int NDT, int TY, int CH>
+template <int NW, int NDT, int TY, int CH, int VAR>
 void launch_swar8(const ProblemDesc &P, unsigned grid, size_t smem,
                   cudaStream_t stream) {
-  swar8_kernel<NW, NDT, TY, CH><<<grid, 32 * TY, smem, stream>>>(P);
+  swar8_kernel<NW, NDT, TY, CH, VAR><<<grid, 32 * TY, smem, stream>>>(P);
 }
 
 template <typename T, int NS, int NDT, int TY, int CH>
@@ -47,27 +47,29 @@ void launch_scalar(const ProblemDesc &P, unsigned grid, size_t smem,
   scalar_kernel<T, NS, NDT, TY, CH><<<grid, 32 * TY, smem, stream>>>(P);
 }
 
-#define DD_SWAR8(NW, NDT, TY, CH)                                             \
-  {"swar8_i" #NW "_d" #NDT "_w" #TY "_c" #CH, kFamilySwar8, 8, 4 * NW, NDT,  \
-   TY, CH, 32 * TY, 128 * NW, TY * NDT,                                       \
-   reinterpret_cast<const void *>(&swar8_kernel<NW, NDT, TY, CH>),           \
-   &launch_swar8<NW, NDT, TY, CH>}
+#define DD_SWAR8(NW, NDT, TY, CH, VAR)                                        \
+  {"swar8_i" #NW "_d" #NDT "_w" #TY "_c" #CH "_v" #VAR, kFamilySwar8, 8,     \
+   4 * NW, NDT, TY, CH, 32 * TY, 128 * NW, TY * NDT, VAR,                    \
+   reinterpret_cast<const void *>(&swar8_kernel<NW, NDT, TY, CH, VAR>),      \
+   &launch_swar8<NW, NDT, TY, CH, VAR>}
 
 #define DD_SCALAR(T, BITS, NS, NDT, TY, CH)                                   \
   {"scalar" #BITS "_i" #NS "_d" #NDT "_w" #TY "_c" #CH, kFamilyScalar, BITS, \
-   NS, NDT, TY, CH, 32 * TY, 32 * NS, TY * NDT,                               \
+   NS, NDT, TY, CH, 32 * TY, 32 * NS, TY * NDT, 0,                            \
    reinterpret_cast<const void *>(&scalar_kernel<T, NS, NDT, TY, CH>),       \
    &launch_scalar<T, NS, NDT, TY, CH>}
 
 static const KernelInfo kRegistry[] = {
-    // swar8: items_t = 4 * NW samples per thread, NDT DMs per thread.
-    DD_SWAR8(4, 4, 8, 8),   // default: 512 samples x 32 DMs, 256 threads
-    DD_SWAR8(4, 4, 8, 16),
-    DD_SWAR8(2, 4, 8, 8),
-    DD_SWAR8(4, 2, 8, 8),
-    DD_SWAR8(2, 8, 8, 8),
-    DD_SWAR8(4, 4, 4, 8),
-    DD_SWAR8(2, 2, 8, 8),
+    // swar8: items_t = 4 * NW samples per thread, NDT DMs per thread,
+    // last argument the inner-loop variant (kUnpackMaskHigh, kUnpackPermute).
+    DD_SWAR8(4, 4, 8, 16, kUnpackMaskHigh),  // default: 512 samples x 32 DMs
+    DD_SWAR8(4, 4, 8, 8, kUnpackMaskHigh),
+    DD_SWAR8(2, 4, 8, 16, kUnpackMaskHigh),
+    DD_SWAR8(4, 2, 8, 16, kUnpackMaskHigh),
+    DD_SWAR8(2, 8, 8, 16, kUnpackMaskHigh),
+    DD_SWAR8(4, 4, 4, 16, kUnpackMaskHigh),
+    DD_SWAR8(4, 4, 8, 16, kUnpackPermute),
+    DD_SWAR8(4, 4, 8, 8, kUnpackPermute),
     // scalar float (float input, step two) and 16-bit.
     DD_SCALAR(float, 32, 8, 4, 8, 8),
     DD_SCALAR(float, 32, 4, 4, 8, 8),

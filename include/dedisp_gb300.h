@@ -230,6 +230,17 @@ dd_status dd_plan_set_shifts(dd_plan *plan, const float *shifts, size_t n);
 dd_status dd_plan_set_zapped(dd_plan *plan, const uint32_t *zapped, size_t n);
 dd_status dd_plan_set_beam_mapping(dd_plan *plan, const uint32_t *mapping,
                                    size_t n);
+/* Compiled tile configurations: how many, and each one's name, input
+ * element width (8 = the 1/2/4/8-bit family) and DedispersionConf. */
+int dd_kernel_count(void);
+dd_status dd_kernel_info(int index, char *name, size_t capacity,
+                         uint32_t *elem_bits, dd_conf *conf);
+/* dd_plan_create with compiled configuration `kernel_index` (the tuner's
+ * entry point: it enumerates configurations by index). */
+dd_status dd_plan_create_with_kernel(dd_plan **plan, const dd_observation *obs,
+                                     dd_mode mode, uint32_t input_bits,
+                                     uint32_t padding, int kernel_index,
+                                     int device);
 /* Enqueue one run on `stream` (a cudaStream_t; NULL = legacy default).
  * Device pointers in the layout dd_get_layout describes; returns after the
  * launch is queued. */
