@@ -60,6 +60,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=2.0,
                     help="target wall time of the CPU baseline sample")
+    ap.add_argument("--kernel-only", action="store_true",
+                    help="run only the warm-up and timed kernel launches (the command ncu "
+                         "captures); prints the device-resident figure alone")
     return ap.parse_args()
 
 
@@ -253,6 +256,14 @@ def main():
     units = world * args.steps * D * S
     value = units / t_dev
     per_launch_s = t_dev / args.steps
+    if args.kernel_only:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+                              "steps": args.steps, "warmup": args.warmup,
+                              "ms_per_step": t_dev / args.steps * 1e3, "kernel_only": True,
+                              "kernel_conf": plan.conf().print(),
+                              "gpu_launches": args.steps * plan.launches()}), flush=True)
+        return
 
     # e2e through the C ABI's synchronous host-buffer call, pinned host memory
     h_in = torch.from_numpy(inp).pin_memory()

@@ -261,11 +261,28 @@ __device__ __forceinline__ void drain_stages(const StageCtx &S, uint32_t sc,
 //   w >> 8 = b1 + 2^8 b2 + 2^16 b3 to a plain 32-bit sum A.  After at most
 //   256 rows A = S1 + 2^8 S2 + 2^16 S3 < 2^32 exactly; S2 is E's high lane, so
 //   A - (S2 << 8) = S1 + 2^16 S3 with S1 < 2^16 splits into S1 and S3.
-enum { kUnpackPermute = 0, kUnpackMaskHigh = 1 };
+// kUnpackPermuteMad: the permutes of kUnpackPermute, with both accumulations
+//   issued as multiply-adds by one on the FMA pipe.
+// kUnpackPermuteHalf: the (b0, b1) accumulation as integer adds, the
+//   (b2, b3) one as multiply-adds, splitting the adds over both pipes.
+enum {
+  kUnpackPermute = 0,
+  kUnpackMaskHigh = 1,
+  kUnpackPermuteMad = 2,
+  kUnpackPermuteHalf = 3
+};
 
 __device__ __forceinline__ uint32_t mad_hi(uint32_t a, uint32_t b, uint32_t c) {
   uint32_t d;
   asm("mad.hi.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+  return d;
+}
+
+// a * b + c on the FMA pipe; with b = 1 (a run-time value, so that the
+// compiler cannot turn it back into an add) it is an add off the ALU pipe.
+__device__ __forceinline__ uint32_t mad_lo(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t d;
+  asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
   return d;
 }
 
@@ -286,6 +303,7 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
   const uint32_t nst = (K + CH - 1) / CH;
   const uint32_t cw = L.copy_words;
   const uint32_t mul = P.mul_hi8;
+  const uint32_t one = P.mul_hi8 >> 24;  // 1, unknown to the compiler
   StageCtx S;
   S.bars = reinterpret_cast<uint64_t *>(smem + L.off_bar);
   S.wstart = reinterpret_cast<uint32_t *>(smem + L.off_wstart);
@@ -317,7 +335,7 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
     for (int j = 0; j < NDT; ++j)
 #pragma unroll
       for (int i = 0; i < NW; ++i) {
-        if (VAR == kUnpackPermute) {
+        if (VAR != kUnpackMaskHigh) {
           tot[j][i][0] += lo[j][i] & 0xFFFFu;
           tot[j][i][1] += lo[j][i] >> 16;
           tot[j][i][2] += hi[j][i] & 0xFFFFu;
@@ -406,9 +424,18 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
           if (VAR == kUnpackPermute) {
             lo[j][i] += __byte_perm(w1, 0, 0x4140) + __byte_perm(w2, 0, 0x4140);
             hi[j][i] += __byte_perm(w1, 0, 0x4342) + __byte_perm(w2, 0, 0x4342);
-          } else {
+          } else if (VAR == kUnpackMaskHigh) {
             lo[j][i] += (w1 & 0x00FF00FFu) + (w2 & 0x00FF00FFu);
             hi[j][i] = mad_hi(w2, mul, mad_hi(w1, mul, hi[j][i]));
+          } else if (VAR == kUnpackPermuteMad) {
+            lo[j][i] = mad_lo(__byte_perm(w2, 0, 0x4140), one,
+                              mad_lo(__byte_perm(w1, 0, 0x4140), one, lo[j][i]));
+            hi[j][i] = mad_lo(__byte_perm(w2, 0, 0x4342), one,
+                              mad_lo(__byte_perm(w1, 0, 0x4342), one, hi[j][i]));
+          } else {
+            lo[j][i] += __byte_perm(w1, 0, 0x4140) + __byte_perm(w2, 0, 0x4140);
+            hi[j][i] = mad_lo(__byte_perm(w2, 0, 0x4342), one,
+                              mad_lo(__byte_perm(w1, 0, 0x4342), one, hi[j][i]));
           }
         }
     }
@@ -419,12 +446,12 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
 #pragma unroll
         for (int i = 0; i < NW; ++i) {
           const uint32_t w = p[32 * i];
-          if (VAR == kUnpackPermute) {
-            lo[j][i] += __byte_perm(w, 0, 0x4140);
-            hi[j][i] += __byte_perm(w, 0, 0x4342);
-          } else {
+          if (VAR == kUnpackMaskHigh) {
             lo[j][i] += w & 0x00FF00FFu;
             hi[j][i] = mad_hi(w, mul, hi[j][i]);
+          } else {
+            lo[j][i] += __byte_perm(w, 0, 0x4140);
+            hi[j][i] += __byte_perm(w, 0, 0x4342);
           }
         }
       }

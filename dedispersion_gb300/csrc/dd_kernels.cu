@@ -62,14 +62,16 @@ void launch_scalar(const ProblemDesc &P, unsigned grid, size_t smem,
 static const KernelInfo kRegistry[] = {
     // swar8: items_t = 4 * NW samples per thread, NDT DMs per thread,
     // last argument the inner-loop variant (kUnpackMaskHigh, kUnpackPermute).
-    DD_SWAR8(4, 4, 8, 16, kUnpackMaskHigh),  // default: 512 samples x 32 DMs
-    DD_SWAR8(4, 4, 8, 8, kUnpackMaskHigh),
-    DD_SWAR8(2, 4, 8, 16, kUnpackMaskHigh),
-    DD_SWAR8(4, 2, 8, 16, kUnpackMaskHigh),
-    DD_SWAR8(2, 8, 8, 16, kUnpackMaskHigh),
-    DD_SWAR8(4, 4, 4, 16, kUnpackMaskHigh),
+    DD_SWAR8(4, 4, 8, 16, kUnpackPermuteMad),  // default: 512 samples x 32 DMs
+    DD_SWAR8(2, 8, 8, 16, kUnpackPermuteMad),
     DD_SWAR8(4, 4, 8, 16, kUnpackPermute),
     DD_SWAR8(4, 4, 8, 8, kUnpackPermute),
+    DD_SWAR8(2, 8, 8, 16, kUnpackPermute),
+    DD_SWAR8(2, 4, 8, 16, kUnpackPermute),
+    DD_SWAR8(4, 2, 8, 16, kUnpackPermute),
+    DD_SWAR8(4, 4, 8, 16, kUnpackPermuteHalf),
+    DD_SWAR8(2, 8, 8, 16, kUnpackPermuteHalf),
+    DD_SWAR8(4, 4, 8, 16, kUnpackMaskHigh),
     // scalar float (float input, step two) and 16-bit.
     DD_SCALAR(float, 32, 8, 4, 8, 8),
     DD_SCALAR(float, 32, 4, 4, 8, 8),
