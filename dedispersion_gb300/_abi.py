@@ -108,6 +108,8 @@ SIGNATURES = {
                                                    C.c_uint32, C.c_uint32]),
     "dd_subband_dedispersion_step_two": (C.c_int, [_OBS, _U32P, _F32P, _F32P, _F32P,
                                                    C.c_uint32]),
+    "dd_dedispersion_noalloc": (C.c_int, [_OBS, _U32P, _U32P, _P, _F32P, _F32P, C.c_uint32,
+                                          C.c_uint32, _P]),
     "dd_plan_create": (C.c_int, [C.POINTER(_P), _OBS, C.c_int, C.c_uint32, C.c_uint32,
                                  _CONF, C.c_int]),
     "dd_kernel_count": (C.c_int, []),

@@ -378,6 +378,11 @@ dd_status rebuild(dd_plan *p) {
 
 }  // namespace
 
+namespace dd {
+// Lets other translation units of the library report through dd_last_error.
+void set_last_error(const char *message) { g_error = message; }
+}  // namespace dd
+
 extern "C" {
 
 const char *dd_last_error(void) { return g_error.c_str(); }

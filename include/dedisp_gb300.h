@@ -211,6 +211,28 @@ dd_status dd_subband_dedispersion_step_two(const dd_observation *obs,
                                            const float *shifts,
                                            uint32_t padding);
 
+/* Single-step dedispersion that allocates no device memory.  It has no
+ * counterpart in the reference.  It is for callers that cannot call
+ * cudaMalloc where they dedisperse: a real-time loop that must not block
+ * (cudaMalloc/cudaFree can synchronize the device), or a framework that owns
+ * all device memory through its own capped pool.  The caller passes device
+ * input and output buffers in the layout of dd_dedispersion and host tables;
+ * the engine's descriptor tables and status word live in one fixed file-scope
+ * device array of about 1 MiB that every GPU loading the library keeps until
+ * exit.  Limits: at most 4096 synthesized beams and 61440 live rows
+ * (synthesized beams x non-zapped channels); larger requests return
+ * DD_ERR_UNSUPPORTED.  The call enqueues on `stream` (a cudaStream_t) and
+ * returns when the output is complete.  The first call on a device looks up
+ * the array's address; make it before capturing any stream.  All calls share
+ * the array, so calls that overlap on the GPU race (host threads are
+ * serialized inside the call). */
+dd_status dd_dedispersion_noalloc(const dd_observation *obs,
+                                  const uint32_t *zapped,
+                                  const uint32_t *beam_mapping,
+                                  const void *d_input, float *d_output,
+                                  const float *shifts, uint32_t padding,
+                                  uint32_t input_bits, void *stream);
+
 /* ---- plans: device-resident tables, asynchronous device-pointer runs ---- */
 /* The device twins of the generated OpenCL kernels `dedispersion`,
  * `dedispersionStepOne`, `dedispersionStepTwo` (include/Dedispersion.hpp:
