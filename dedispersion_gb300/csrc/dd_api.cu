@@ -237,6 +237,12 @@ struct dd_plan {
   dd::EntryDesc *d_entries = nullptr;
   size_t cap_groups = 0, cap_entries = 0;
   uint32_t *d_status = nullptr;
+  // Precomputed delays (ProblemDesc::delay_base / delay_rel).
+  std::vector<float> delay_shift;  // delay per unit DM of each delay row
+  std::vector<uint16_t> delay_rel;
+  uint16_t *d_delay_rel = nullptr;
+  size_t cap_delay_rel = 0;
+  bool use_delay_tables = false;
   bool ready = false;
 };
 
@@ -251,12 +257,18 @@ dd_status rebuild(dd_plan *p) {
   const uint32_t C = o->nr_channels;
   p->groups.clear();
   p->entries.clear();
+  p->delay_shift.clear();
   auto zapped = [&](uint32_t c) { return !p->zapped.empty() && p->zapped[c] != 0; };
+  // Entries of a group take consecutive delay rows; groups with the same
+  // delays per unit DM share rows.
   if (p->mode == DD_SINGLE_STEP) {
     p->nr_groups = o->nr_synthesized_beams;
     p->out_dm_stride = d.out_row;
+    for (uint32_t c = 0; c < C; c++)
+      if (!zapped(c)) p->delay_shift.push_back(p->shifts[c]);
     for (uint32_t g = 0; g < p->nr_groups; g++) {
       dd::GroupDesc G{(uint32_t)p->entries.size(), 0, (uint64_t)g * d.nr_dms * d.out_row};
+      uint32_t row = 0;
       for (uint32_t c = 0; c < C; c++) {
         if (zapped(c)) continue;
         uint64_t beam = p->mapping.empty() ? (o->nr_beams ? g % o->nr_beams : 0)
@@ -264,7 +276,7 @@ dd_status rebuild(dd_plan *p) {
         if (beam >= o->nr_beams)
           return fail(DD_ERR_INVALID_ARGUMENT, "beam mapping[%u][%u] = %llu >= nr_beams %u",
                       g, c, (unsigned long long)beam, o->nr_beams);
-        p->entries.push_back({(beam * C + c) * d.row_bytes, p->shifts[c], 0});
+        p->entries.push_back({(beam * C + c) * d.row_bytes, p->shifts[c], row++});
       }
       G.entry_count = (uint32_t)p->entries.size() - G.entry_begin;
       p->groups.push_back(G);
@@ -273,15 +285,25 @@ dd_status rebuild(dd_plan *p) {
     const uint32_t SB = o->nr_subbands, cps = C / SB;
     p->nr_groups = o->nr_beams * SB;
     p->out_dm_stride = (uint64_t)SB * d.out_row;
+    std::vector<uint32_t> sb_row(SB);
+    for (uint32_t sb = 0; sb < SB; sb++) {
+      sb_row[sb] = (uint32_t)p->delay_shift.size();
+      const float last = p->shifts[(sb + 1) * cps - 1];
+      for (uint32_t c = sb * cps; c < (sb + 1) * cps; c++) {
+        if (zapped(c)) continue;
+        volatile float rel = p->shifts[c] - last;
+        p->delay_shift.push_back(static_cast<float>(rel));
+      }
+    }
     for (uint32_t b = 0; b < o->nr_beams; b++)
       for (uint32_t sb = 0; sb < SB; sb++) {
         dd::GroupDesc G{(uint32_t)p->entries.size(), 0,
                         ((uint64_t)b * d.nr_dms * SB + sb) * d.out_row};
-        const float last = p->shifts[(sb + 1) * cps - 1];
+        uint32_t row = sb_row[sb];
         for (uint32_t c = sb * cps; c < (sb + 1) * cps; c++) {
           if (zapped(c)) continue;
-          volatile float rel = p->shifts[c] - last;
-          p->entries.push_back({((uint64_t)b * C + c) * d.row_bytes, rel, 0});
+          p->entries.push_back({((uint64_t)b * C + c) * d.row_bytes, p->delay_shift[row], row});
+          row++;
         }
         G.entry_count = (uint32_t)p->entries.size() - G.entry_begin;
         p->groups.push_back(G);
@@ -290,6 +312,7 @@ dd_status rebuild(dd_plan *p) {
     const uint32_t SB = o->nr_subbands, D1 = o->nr_dms_subbanding;
     p->nr_groups = o->nr_synthesized_beams * D1;
     p->out_dm_stride = d.out_row;
+    for (uint32_t sb = 0; sb < SB; sb++) p->delay_shift.push_back(p->shifts[sb]);
     for (uint32_t g = 0; g < o->nr_synthesized_beams; g++)
       for (uint32_t d1 = 0; d1 < D1; d1++) {
         dd::GroupDesc G{(uint32_t)p->entries.size(), SB,
@@ -300,7 +323,7 @@ dd_status rebuild(dd_plan *p) {
           if (beam >= o->nr_beams)
             return fail(DD_ERR_INVALID_ARGUMENT, "beam mapping[%u][%u] = %llu >= nr_beams %u",
                         g, s, (unsigned long long)beam, o->nr_beams);
-          p->entries.push_back({((beam * D1 + d1) * SB + s) * d.row_bytes, p->shifts[s], 0});
+          p->entries.push_back({((beam * D1 + d1) * SB + s) * d.row_bytes, p->shifts[s], s});
         }
         p->groups.push_back(G);
       }
@@ -331,6 +354,25 @@ dd_status rebuild(dd_plan *p) {
     return fail(DD_ERR_INVALID_ARGUMENT,
                 "rows hold %u samples but %u output samples + max delay %u are needed",
                 d.row_samples, d.nr_samples, max_delay);
+  // Delay table: the offsets of each DM tile's delays from the delay of its
+  // first DM, per delay row (the same float order as the device's
+  // dev_delay).  16-bit offsets: skipped if a spread does not fit.
+  const size_t rows = p->delay_shift.size();
+  p->use_delay_tables = spread < 65536 && rows > 0 && p->tiles_d > 0;
+  if (p->use_delay_tables) {
+    p->delay_rel.assign((size_t)p->tiles_d * rows * k.tile_d, 0);
+    for (uint32_t t = 0; t < p->tiles_d; t++)
+      for (size_t r = 0; r < rows; r++) {
+        const float sh = p->delay_shift[r];
+        const uint32_t d0 = t * k.tile_d;
+        const uint32_t base = dd::host_delay(d.first_dm, d.dm_step, d0, sh);
+        uint16_t *rel = &p->delay_rel[((size_t)t * rows + r) * k.tile_d];
+        for (int j = 0; j < k.tile_d; j++) {
+          const uint32_t dm = std::min(d0 + (uint32_t)j, d.nr_dms - 1);
+          rel[j] = (uint16_t)(dd::host_delay(d.first_dm, d.dm_step, dm, sh) - base);
+        }
+      }
+  }
   const uint32_t bits = family_bits(p->mode, p->bits) == 8 ? p->bits : family_bits(p->mode, p->bits);
   const uint32_t a = dd::window_alignment_samples(bits);
   p->win = ((k.tile_t + spread + a + 8) + 15) / 16 * 16;
@@ -368,6 +410,18 @@ dd_status rebuild(dd_plan *p) {
   if (!p->entries.empty())
     DD_CUDA(cudaMemcpy(p->d_entries, p->entries.data(), p->entries.size() * sizeof(dd::EntryDesc),
                        cudaMemcpyHostToDevice), "upload entry table");
+  if (p->use_delay_tables) {
+    if (p->delay_rel.size() > p->cap_delay_rel) {
+      if (p->d_delay_rel) cudaFree(p->d_delay_rel);
+      p->d_delay_rel = nullptr;
+      DD_CUDA(cudaMalloc(&p->d_delay_rel, p->delay_rel.size() * sizeof(uint16_t)),
+              "allocate delay table");
+      p->cap_delay_rel = p->delay_rel.size();
+    }
+    DD_CUDA(cudaMemcpy(p->d_delay_rel, p->delay_rel.data(),
+                       p->delay_rel.size() * sizeof(uint16_t), cudaMemcpyHostToDevice),
+            "upload delay table");
+  }
   // The attribute is a cap shared by every plan of this kernel: set it to the
   // device maximum so that no plan lowers it below another plan's need.
   DD_CUDA(cudaFuncSetAttribute(k.func, cudaFuncAttributeMaxDynamicSharedMemorySize, dev_max),
@@ -682,6 +736,10 @@ dd_status dd_plan_run(dd_plan *p, const void *d_input, float *d_output, void *st
   P.tma = (d.row_bytes % 16 == 0 && reinterpret_cast<uintptr_t>(d_input) % 16 == 0) ? 1u : 0u;
   P.out_vec4 = (d.out_row % 4 == 0 && reinterpret_cast<uintptr_t>(d_output) % 16 == 0) ? 1u : 0u;
   P.mul_hi8 = 1u << 24;
+  if (p->use_delay_tables) {
+    P.delay_rows = (uint32_t)p->delay_shift.size();
+    P.delay_rel = p->d_delay_rel;
+  }
   DeviceGuard g(p->device);
   if (!g.ok) return fail(DD_ERR_CUDA, "cannot select device %d", p->device);
   p->kinfo->launch(P, (unsigned)tiles, p->smem, static_cast<cudaStream_t>(stream));
@@ -723,6 +781,7 @@ dd_status dd_plan_destroy(dd_plan *p) {
     if (p->d_groups) cudaFree(p->d_groups);
     if (p->d_entries) cudaFree(p->d_entries);
     if (p->d_status) cudaFree(p->d_status);
+    if (p->d_delay_rel) cudaFree(p->d_delay_rel);
   }
   delete p;
   return DD_OK;

@@ -72,7 +72,7 @@ __host__ __device__ inline SmemLayout make_layout(int family, uint32_t win,
   }
   L.off_bar = 0;
   L.off_wstart = 64;
-  L.off_table = round_up(L.off_wstart + kNRaw * ch * 4u, 128u);
+  L.off_table = round_up(L.off_wstart + 2u * kNRaw * ch * 4u, 128u);
   L.off_raw = round_up(L.off_table + 2u * ch * tile_d * 4u, 128u);
   L.off_copy = round_up(L.off_raw + kNRaw * ch * L.raw_bytes, 128u);
   L.total = L.off_copy + 2u * ch * 4u * L.copy_words * 4u;
@@ -181,7 +181,8 @@ __device__ __forceinline__ uint32_t expand_word(const uint8_t *row, uint32_t k,
 
 struct StageCtx {
   uint64_t *bars;
-  uint32_t *wstart;
+  uint32_t *wstart;  // first staged sample of each row of a slot
+  uint32_t *wmod;    // t0 + delay(row, first DM of the tile) - wstart
   uint8_t *raw;
   uint32_t raw_bytes;
 };
@@ -193,7 +194,8 @@ __device__ __forceinline__ void issue_stage(const ProblemDesc &P,
                                             const GroupDesc &G,
                                             const StageCtx &S, uint32_t s,
                                             uint32_t gs, uint32_t t0,
-                                            uint32_t d0, int lane) {
+                                            uint32_t d0, uint32_t dtile,
+                                            int lane) {
   if (lane >= CH) return;
   const uint32_t slot = gs % kNRaw;
   uint64_t *bar = S.bars + slot;
@@ -204,8 +206,13 @@ __device__ __forceinline__ void issue_stage(const ProblemDesc &P,
   }
   const EntryDesc E = P.entries[G.entry_begin + e];
   const uint32_t a = align_samples(P.bits);
-  const uint32_t ws = (t0 + dev_delay(P.first_dm, P.dm_step, d0, E.shift)) / a * a;
+  // One delay per row and stage: computed here rather than loaded, keeping
+  // global latency off the issuing warp (equal to the host's delay_base).
+  (void)dtile;
+  const uint32_t base = dev_delay(P.first_dm, P.dm_step, d0, E.shift);
+  const uint32_t ws = (t0 + base) / a * a;
   S.wstart[slot * CH + lane] = ws;
+  S.wmod[slot * CH + lane] = t0 + base - ws;
   if (P.tma) {
     const uint64_t boff = P.bits <= 8 ? (uint64_t)ws * P.bits / 8u
                                       : (uint64_t)ws * (P.bits / 8u);
@@ -218,6 +225,54 @@ __device__ __forceinline__ void issue_stage(const ProblemDesc &P,
   } else {
     mbar_arrive(bar);
   }
+}
+
+// Start of the precomputed relative delays of stage s (NULL if absent).
+__device__ __forceinline__ const uint16_t *stage_rel(const ProblemDesc &P,
+                                                     const GroupDesc &G,
+                                                     uint32_t s, int CH,
+                                                     uint32_t dtile, int tile_d) {
+  if (!P.delay_rel) return nullptr;
+  const uint32_t row0 = P.entries[G.entry_begin + s * CH].delay_row;
+  return P.delay_rel + ((size_t)dtile * P.delay_rows + row0) * tile_d;
+}
+
+// The (row, DM) table entries of one stage that a thread fills, and the
+// precomputed delays for them, loaded one stage ahead so that their global
+// latency hides behind the current stage's sums.  Entry idx = tid + r * THREADS.
+template <int CH, int TILE_D, int THREADS>
+struct StageDelays {
+  static constexpr int R = (CH * TILE_D + THREADS - 1) / THREADS;
+  uint32_t v[R];
+
+  __device__ __forceinline__ void load(const ProblemDesc &P, const GroupDesc &G, uint32_t s,
+                                       uint32_t dtile, uint32_t cnt) {
+    const uint16_t *rel = stage_rel(P, G, s, CH, dtile, TILE_D);
+    if (!rel) return;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const uint32_t idx = threadIdx.x + r * THREADS;
+      v[r] = idx < cnt * TILE_D ? rel[idx] : 0u;
+    }
+  }
+
+  // Sample offset of entry r from the start of its row's staged window.
+  __device__ __forceinline__ uint32_t offset(const ProblemDesc &P, const GroupDesc &G,
+                                             const StageCtx &S, int r, uint32_t s,
+                                             uint32_t slot, uint32_t t0, uint32_t d0) const {
+    const uint32_t idx = threadIdx.x + r * THREADS;
+    const uint32_t ch = idx / TILE_D, j = idx % TILE_D;
+    if (P.delay_rel) return v[r] + S.wmod[slot * CH + ch];
+    const uint32_t d = (d0 + j) < P.nr_dms ? (d0 + j) : (P.nr_dms - 1);
+    const float sh = P.entries[G.entry_begin + s * CH + ch].shift;
+    return t0 + dev_delay(P.first_dm, P.dm_step, d, sh) - S.wstart[slot * CH + ch];
+  }
+};
+
+__device__ __forceinline__ uint32_t lds_u32(uint32_t addr) {
+  uint32_t v;
+  asm volatile("ld.shared.b32 %0, [%1];" : "=r"(v) : "r"(addr));
+  return v;
 }
 
 // Without bulk copies (unaligned rows): the CTA copies the windows of one
@@ -307,6 +362,7 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
   StageCtx S;
   S.bars = reinterpret_cast<uint64_t *>(smem + L.off_bar);
   S.wstart = reinterpret_cast<uint32_t *>(smem + L.off_wstart);
+  S.wmod = S.wstart + kNRaw * CH;
   S.raw = smem + L.off_raw;
   S.raw_bytes = L.raw_bytes;
   uint32_t *table = reinterpret_cast<uint32_t *>(smem + L.off_table);
@@ -315,7 +371,7 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
   if (ty == 0) {
     const uint32_t pro = nst < (uint32_t)kNRaw ? nst : (uint32_t)kNRaw;
     for (uint32_t s = 0; s < pro; ++s)
-      issue_stage<CH>(P, G, S, s, sc + s, t0, d0, tx);
+      issue_stage<CH>(P, G, S, s, sc + s, t0, d0, dtile, tx);
   }
 
   // kUnpackPermute: lo = (b0, b1) lanes, hi = (b2, b3) lanes.
@@ -329,6 +385,9 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
       tot[j][i][0] = tot[j][i][1] = tot[j][i][2] = tot[j][i][3] = 0;
     }
   uint32_t since = 0;
+  using Delays = StageDelays<CH, kTileD, kThreads>;
+  Delays delays;
+  if (nst) delays.load(P, G, 0, dtile, K < (uint32_t)CH ? K : CH);
 
   auto flush = [&]() {
 #pragma unroll
@@ -360,35 +419,43 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
       copy_stage_plain<CH, TY>(P, G, S, s, slot, cnt);
       __syncthreads();
     }
-    // Expand to bytes and write the four shifted copies of each row.
+    // Expand to bytes and write the four shifted copies of each row, two
+    // words per thread and step (copy m word k = samples 4k+m .. 4k+m+3).
     uint32_t *ac = copies + area * (CH * 4u * cw);
     for (uint32_t ch = ty; ch < cnt; ch += TY) {
       const uint8_t *r = S.raw + (slot * CH + ch) * S.raw_bytes;
       uint32_t *dst = ac + ch * 4u * cw;
-      for (uint32_t k = tx; k < cw; k += 32) {
-        uint32_t w0, w1;
+      for (uint32_t k = 2 * tx; k < cw; k += 64) {
+        uint32_t w0, w1, w2;
         if (P.bits == 8) {
-          w0 = reinterpret_cast<const uint32_t *>(r)[k];
-          w1 = reinterpret_cast<const uint32_t *>(r)[k + 1];
+          const uint2 v = *reinterpret_cast<const uint2 *>(r + 4 * k);
+          w0 = v.x;
+          w1 = v.y;
+          w2 = reinterpret_cast<const uint32_t *>(r)[k + 2];
         } else {
           w0 = expand_word(r, k, P.bits);
           w1 = expand_word(r, k + 1, P.bits);
+          w2 = expand_word(r, k + 2, P.bits);
         }
-        dst[k] = w0;
-        dst[cw + k] = __funnelshift_r(w0, w1, 8);
-        dst[2 * cw + k] = __funnelshift_r(w0, w1, 16);
-        dst[3 * cw + k] = __funnelshift_r(w0, w1, 24);
+        *reinterpret_cast<uint2 *>(dst + k) = make_uint2(w0, w1);
+        *reinterpret_cast<uint2 *>(dst + cw + k) =
+            make_uint2(__funnelshift_r(w0, w1, 8), __funnelshift_r(w1, w2, 8));
+        *reinterpret_cast<uint2 *>(dst + 2 * cw + k) =
+            make_uint2(__funnelshift_r(w0, w1, 16), __funnelshift_r(w1, w2, 16));
+        *reinterpret_cast<uint2 *>(dst + 3 * cw + k) =
+            make_uint2(__funnelshift_r(w0, w1, 24), __funnelshift_r(w1, w2, 24));
       }
     }
-    // Word index of (row, DM) in the copy area: copy (o & 3), word (o >> 2).
+    // Byte offset of (row, DM) in the copy area: copy (o & 3), word (o >> 2).
     uint32_t *tb = table + area * (CH * kTileD);
-    for (uint32_t idx = tid; idx < cnt * kTileD; idx += kThreads) {
-      const uint32_t ch = idx / kTileD, j = idx % kTileD;
-      const uint32_t d = (d0 + j) < P.nr_dms ? (d0 + j) : (P.nr_dms - 1);
-      const float sh = P.entries[G.entry_begin + s * CH + ch].shift;
-      const uint32_t o = t0 + dev_delay(P.first_dm, P.dm_step, d, sh) -
-                         S.wstart[slot * CH + ch];
-      tb[idx] = ch * 4u * cw + (o & 3u) * cw + (o >> 2);
+#pragma unroll
+    for (int r = 0; r < Delays::R; ++r) {
+      const uint32_t idx = tid + r * kThreads;
+      if (idx < cnt * kTileD) {
+        const uint32_t ch = idx / kTileD;
+        const uint32_t o = delays.offset(P, G, S, r, s, slot, t0, d0);
+        tb[idx] = 4u * (ch * 4u * cw + (o & 3u) * cw + (o >> 2));
+      }
     }
     if (__syncthreads_or(!ok)) {
       if (tid == 0) atomicOr(P.status, kStatusTimeout);
@@ -397,7 +464,9 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
       return false;
     }
     if (ty == 0 && s + kNRaw < nst)
-      issue_stage<CH>(P, G, S, s + kNRaw, gs + kNRaw, t0, d0, tx);
+      issue_stage<CH>(P, G, S, s + kNRaw, gs + kNRaw, t0, d0, dtile, tx);
+    if (s + 1 < nst)
+      delays.load(P, G, s + 1, dtile, (K - (s + 1) * CH) < (uint32_t)CH ? (K - (s + 1) * CH) : CH);
 
     if (since + cnt > 256u) {
       flush();
@@ -405,22 +474,23 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
     }
     since += cnt;
 
+    // 32-bit shared addresses: one add per (row, DM), immediates per word.
     const uint32_t *tbt = tb + ty * NDT;
-    const uint32_t *act = ac + tx;
+    const uint32_t acs = smem_addr(ac) + 4u * tx;
     uint32_t ch = 0;
     for (; ch + 1 < cnt; ch += 2) {
-      const uint32_t *p1[NDT], *p2[NDT];
+      uint32_t p1[NDT], p2[NDT];
 #pragma unroll
       for (int j = 0; j < NDT; ++j) {
-        p1[j] = act + tbt[ch * kTileD + j];
-        p2[j] = act + tbt[(ch + 1) * kTileD + j];
+        p1[j] = acs + tbt[ch * kTileD + j];
+        p2[j] = acs + tbt[(ch + 1) * kTileD + j];
       }
 #pragma unroll
       for (int j = 0; j < NDT; ++j)
 #pragma unroll
         for (int i = 0; i < NW; ++i) {
-          const uint32_t w1 = p1[j][32 * i];
-          const uint32_t w2 = p2[j][32 * i];
+          const uint32_t w1 = lds_u32(p1[j] + 128u * i);
+          const uint32_t w2 = lds_u32(p2[j] + 128u * i);
           if (VAR == kUnpackPermute) {
             lo[j][i] += __byte_perm(w1, 0, 0x4140) + __byte_perm(w2, 0, 0x4140);
             hi[j][i] += __byte_perm(w1, 0, 0x4342) + __byte_perm(w2, 0, 0x4342);
@@ -442,10 +512,10 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
     if (ch < cnt) {
 #pragma unroll
       for (int j = 0; j < NDT; ++j) {
-        const uint32_t *p = act + tbt[ch * kTileD + j];
+        const uint32_t p = acs + tbt[ch * kTileD + j];
 #pragma unroll
         for (int i = 0; i < NW; ++i) {
-          const uint32_t w = p[32 * i];
+          const uint32_t w = lds_u32(p + 128u * i);
           if (VAR == kUnpackMaskHigh) {
             lo[j][i] += w & 0x00FF00FFu;
             hi[j][i] = mad_hi(w, mul, hi[j][i]);
@@ -497,6 +567,22 @@ struct ScalarAcc<float> {
   using type = float;
 };
 
+// Element load from a 32-bit shared address, widened to the accumulator.
+template <typename T>
+__device__ __forceinline__ typename ScalarAcc<T>::type lds_elem(uint32_t addr);
+template <>
+__device__ __forceinline__ uint32_t lds_elem<uint16_t>(uint32_t addr) {
+  uint32_t v;
+  asm volatile("ld.shared.u16 %0, [%1];" : "=r"(v) : "r"(addr));
+  return v;
+}
+template <>
+__device__ __forceinline__ float lds_elem<float>(uint32_t addr) {
+  float v;
+  asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(addr));
+  return v;
+}
+
 template <typename T, int NS, int NDT, int TY, int CH>
 __device__ __forceinline__ bool scalar_tile(const ProblemDesc &P,
                                             const GroupDesc &G, uint32_t dtile,
@@ -512,19 +598,19 @@ __device__ __forceinline__ bool scalar_tile(const ProblemDesc &P,
   const uint32_t t0 = ttile * kTileT, d0 = dtile * kTileD;
   const uint32_t K = G.entry_count;
   const uint32_t nst = (K + CH - 1) / CH;
-  const uint32_t slot_elems = L.raw_bytes / sizeof(T);
   StageCtx S;
   S.bars = reinterpret_cast<uint64_t *>(smem + L.off_bar);
   S.wstart = reinterpret_cast<uint32_t *>(smem + L.off_wstart);
+  S.wmod = S.wstart + kNRaw * CH;
   S.raw = smem + L.off_raw;
   S.raw_bytes = L.raw_bytes;
   uint32_t *table = reinterpret_cast<uint32_t *>(smem + L.off_table);
-  const T *rawt = reinterpret_cast<const T *>(S.raw);
+  const uint32_t raws = smem_addr(S.raw) + (uint32_t)sizeof(T) * tx;
 
   if (ty == 0) {
     const uint32_t pro = nst < (uint32_t)kAhead ? nst : (uint32_t)kAhead;
     for (uint32_t s = 0; s < pro; ++s)
-      issue_stage<CH>(P, G, S, s, sc + s, t0, d0, tx);
+      issue_stage<CH>(P, G, S, s, sc + s, t0, d0, dtile, tx);
   }
 
   Acc acc[NDT][NS];
@@ -532,6 +618,9 @@ __device__ __forceinline__ bool scalar_tile(const ProblemDesc &P,
   for (int j = 0; j < NDT; ++j)
 #pragma unroll
     for (int i = 0; i < NS; ++i) acc[j][i] = Acc(0);
+  using Delays = StageDelays<CH, kTileD, kThreads>;
+  Delays delays;
+  if (nst) delays.load(P, G, 0, dtile, K < (uint32_t)CH ? K : CH);
 
   for (uint32_t s = 0; s < nst; ++s) {
     const uint32_t gs = sc + s, slot = gs % kNRaw, area = gs & 1u;
@@ -541,15 +630,19 @@ __device__ __forceinline__ bool scalar_tile(const ProblemDesc &P,
       copy_stage_plain<CH, TY>(P, G, S, s, slot, cnt);
       __syncthreads();
     }
+    // Byte offset of (row, DM) from the start of the raw slots.
     uint32_t *tb = table + area * (CH * kTileD);
-    for (uint32_t idx = tid; idx < cnt * kTileD; idx += kThreads) {
-      const uint32_t ch = idx / kTileD, j = idx % kTileD;
-      const uint32_t d = (d0 + j) < P.nr_dms ? (d0 + j) : (P.nr_dms - 1);
-      const float sh = P.entries[G.entry_begin + s * CH + ch].shift;
-      const uint32_t o = t0 + dev_delay(P.first_dm, P.dm_step, d, sh) -
-                         S.wstart[slot * CH + ch];
-      tb[idx] = (slot * CH + ch) * slot_elems + o;
+#pragma unroll
+    for (int r = 0; r < Delays::R; ++r) {
+      const uint32_t idx = tid + r * kThreads;
+      if (idx < cnt * kTileD) {
+        const uint32_t ch = idx / kTileD;
+        const uint32_t o = delays.offset(P, G, S, r, s, slot, t0, d0);
+        tb[idx] = (slot * CH + ch) * L.raw_bytes + (uint32_t)sizeof(T) * o;
+      }
     }
+    if (s + 1 < nst)
+      delays.load(P, G, s + 1, dtile, (K - (s + 1) * CH) < (uint32_t)CH ? (K - (s + 1) * CH) : CH);
     if (__syncthreads_or(!ok)) {
       if (tid == 0) atomicOr(P.status, kStatusTimeout);
       const uint32_t last = (s + kAhead) < nst ? (s + kAhead) : nst;
@@ -557,17 +650,18 @@ __device__ __forceinline__ bool scalar_tile(const ProblemDesc &P,
       return false;
     }
     if (ty == 0 && s + kAhead < nst)
-      issue_stage<CH>(P, G, S, s + kAhead, gs + kAhead, t0, d0, tx);
+      issue_stage<CH>(P, G, S, s + kAhead, gs + kAhead, t0, d0, dtile, tx);
 
     const uint32_t *tbt = tb + ty * NDT;
     for (uint32_t ch = 0; ch < cnt; ++ch) {
       uint32_t b[NDT];
 #pragma unroll
-      for (int j = 0; j < NDT; ++j) b[j] = tbt[ch * kTileD + j] + tx;
+      for (int j = 0; j < NDT; ++j) b[j] = raws + tbt[ch * kTileD + j];
 #pragma unroll
       for (int j = 0; j < NDT; ++j)
 #pragma unroll
-        for (int i = 0; i < NS; ++i) acc[j][i] += Acc(rawt[b[j] + 32 * i]);
+        for (int i = 0; i < NS; ++i)
+          acc[j][i] += lds_elem<T>(b[j] + (uint32_t)(32 * sizeof(T)) * i);
     }
   }
   sc += nst;

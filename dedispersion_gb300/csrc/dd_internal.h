@@ -34,7 +34,7 @@ struct GroupDesc {
 struct EntryDesc {
   uint64_t row_offset;  // byte offset of the row from the input base
   float shift;          // delay in samples per unit DM
-  uint32_t reserved;
+  uint32_t delay_row;   // row of the precomputed delay tables (when present)
 };
 
 // Device status word bits, set with atomicOr by a kernel.
@@ -63,6 +63,12 @@ struct ProblemDesc {
   uint32_t tma;            // 1: rows staged by bulk async copies
   uint32_t out_vec4;       // 1: float4 stores are aligned
   uint32_t mul_hi8;        // always 1 << 24 (w >> 8 as a high-half multiply)
+  uint32_t delay_rows;     // rows of the delay table below
+  // Optional precomputed delays (NULL: computed on the device).  For DM
+  // tile t (first DM d0), delay row r and j < tile_d:
+  //   delay_rel[(t * delay_rows + r) * tile_d + j]
+  //       = delay(r, min(d0 + j, nr_dms - 1)) - delay(r, d0)
+  const uint16_t *delay_rel;
 };
 
 // One entry of the kernel registry: a compiled tile configuration.

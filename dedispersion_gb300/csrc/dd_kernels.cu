@@ -14,7 +14,7 @@ namespace dd {
 
 // Grid-mapped kernel: one CTA per tile.
 template <int NW, int NDT, int TY, int CH, int VAR>
-__global__ void __launch_bounds__(32 * TY, (TY >= 8 ? 2 : 4))
+__global__ void __launch_bounds__(32 * TY, (TY >= 16 ? 1 : (TY >= 8 ? 2 : 4)))
     swar8_kernel(const ProblemDesc P) {
   extern __shared__ __align__(128) uint8_t smem[];
   const SmemLayout L = make_layout(kFamilySwar8, P.win_samples, P.bits, CH, TY * NDT);
@@ -64,6 +64,7 @@ static const KernelInfo kRegistry[] = {
     // last argument the inner-loop variant (kUnpackMaskHigh, kUnpackPermute).
     DD_SWAR8(4, 4, 8, 16, kUnpackPermuteMad),  // default: 512 samples x 32 DMs
     DD_SWAR8(2, 8, 8, 16, kUnpackPermuteMad),
+    DD_SWAR8(4, 4, 16, 16, kUnpackPermuteMad),
     DD_SWAR8(4, 4, 8, 16, kUnpackPermute),
     DD_SWAR8(4, 4, 8, 8, kUnpackPermute),
     DD_SWAR8(2, 8, 8, 16, kUnpackPermute),

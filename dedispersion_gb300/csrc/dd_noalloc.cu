@@ -153,7 +153,7 @@ extern "C" dd_status dd_dedispersion_noalloc(const dd_observation *o, const uint
         return fail(DD_ERR_INVALID_ARGUMENT, "shift[%u] must be finite and >= 0", c);
       entries[ne].row_offset = (beam * C + c) * row_bytes;
       entries[ne].shift = sh;
-      entries[ne].reserved = 0;
+      entries[ne].delay_row = 0;
       ne++;
     }
     groups[g].entry_count = ne - groups[g].entry_begin;
