@@ -55,11 +55,13 @@ LANES = 128
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=2.0,
                     help="target wall time of the CPU baseline sample")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the 40-beam batched measurement")
     ap.add_argument("--kernel-only", action="store_true",
                     help="run only the warm-up and timed kernel launches (the command ncu "
                          "captures); prints the device-resident figure alone")
@@ -164,6 +166,71 @@ def cpu_sample(obs, shifts, zapped, mapping, inp, target_s, threads):
 def dd_out_row(obs):
     import dedispersion_gb300 as dd
     return dd.pad(obs.getNrSamplesPerBatch(), PADDING // 4)
+
+
+def bench_batched(torch, device: int, reps: int = 3, count: int = 40):
+    """40 uneven beams (384/1536 ch, 8192-32768 samples, 512-4096 DMs, steps
+    0.1-0.5, 2/4/8-bit uniform input) in one persistent launch replayed from a
+    CUDA graph, against the same beams launched one plain kernel each."""
+    import dedispersion_gb300 as dd
+    from dedispersion_gb300 import synthetic as syn
+    padding = PADDING
+    shapes = syn.batched_shapes(count)
+    batch = dd.Batch(device)
+    beams = []
+    units = 0
+    for sh in shapes:
+        obs = syn.shape_observation(sh, padding)
+        shifts = dd.getShifts(obs, padding)
+        zapped = syn.zapped_mask(sh["channels"], 0.05, sh["seed"], padding)
+        mapping = syn.identity_mapping(obs, padding)
+        d_in = syn.device_uniform_input(torch, obs, sh["bits"], padding, sh["seed"])
+        lay = dd.layout(obs, dd.DD_SINGLE_STEP, sh["bits"], padding)
+        d_out = torch.empty(lay.output_bytes // 4, dtype=torch.float32, device=f"cuda:{device}")
+        d_ref = torch.empty_like(d_out)
+        batch.add(obs, sh["bits"], padding, shifts, zapped, mapping, d_in, d_out)
+        plan = dd.Plan(obs, dd.DD_SINGLE_STEP, sh["bits"], padding, device=device)
+        plan.setShifts(shifts)
+        plan.setZappedChannels(zapped)
+        plan.setBeamMapping(mapping)
+        beams.append((obs, lay, d_in, d_out, d_ref, plan))
+        units += obs.getNrDMs() * obs.getNrSamplesPerBatch()
+    batch.commit()
+    stream = torch.cuda.current_stream()
+    batch.run(stream)
+    batch.check(stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        batch.run(stream)
+    e1.record(stream)
+    batch.check(stream)
+    t_batch = e0.elapsed_time(e1) / 1e3 / reps
+    for b in beams:
+        b[5].run(b[2], b[4], stream)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        for b in beams:
+            b[5].run(b[2], b[4], stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_plain = e0.elapsed_time(e1) / 1e3 / reps
+    exact = True
+    for obs, lay, d_in, d_out, d_ref, plan in beams:
+        S = obs.getNrSamplesPerBatch()
+        rows = lay.output_bytes // 4 // lay.output_row_elems
+        exact &= bool(torch.equal(d_out.view(rows, -1)[:, :S], d_ref.view(rows, -1)[:, :S]))
+        plan.close()
+    info = batch.info()
+    batch.close()
+    return {"value": units / t_batch, "unit": UNIT, "ms_per_batch": t_batch * 1e3,
+            "plain_sequential_value": units / t_plain, "plain_sequential_ms": t_plain * 1e3,
+            "speedup_vs_plain": t_plain / t_batch, "beams": count, "tiles": info["tiles"],
+            "persistent_ctas": info["grid"], "bit_exact_vs_plain": exact,
+            "launch": "one persistent kernel replayed from a CUDA graph",
+            "workload": "40 beams: 384/1536 ch, 8192-32768 samples, 512-4096 DMs, DM step "
+                        "0.1-0.5, 2/4/8-bit uniform input, 5% zapped"}
 
 
 def run_reference(args, rank, world):
@@ -284,6 +351,8 @@ def main():
         t_e2e = float(tt.item())
     e2e_value = world * e2e_steps * D * S / t_e2e
 
+    batched = bench_batched(torch, local) if not args.no_batched else None
+
     if rank != 0:
         return
     # roofline of the plain kernel
@@ -329,6 +398,7 @@ def main():
                                    f"channels), {cpu_dt:.2f} s wall on {cpu_threads} threads"},
         "clocks": clocks,
         "gpu_launches": args.steps * plan.launches(),
+        "batched": batched,
     }
     print(json.dumps(line), flush=True)
     if pg is not None:

@@ -375,6 +375,53 @@ def _stream(s) -> int:
     return int(getattr(s, "cuda_stream"))
 
 
+class Batch:
+    """Many single-step problems (1/2/4/8-bit) in one persistent launch,
+    recorded as a CUDA graph at commit().  Device buffers are bound by add()."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        check(lib().dd_batch_create(C.byref(self._h), device))
+        self._keep = []
+
+    def add(self, observation: Observation, inputBits: int, padding: int, shifts, zapped,
+            mapping, d_input, d_output) -> int:
+        sh = np.ascontiguousarray(shifts, dtype=np.float32)
+        z, m = _u32(zapped), _u32(mapping)
+        idx = C.c_uint32(0)
+        check(lib().dd_batch_add(self._h, C.byref(observation.c), inputBits, padding,
+                                 _ptr(sh, C.c_float), _ptr(z, C.c_uint32), _ptr(m, C.c_uint32),
+                                 C.c_void_p(_devptr(d_input)), C.c_void_p(_devptr(d_output)),
+                                 C.byref(idx)))
+        self._keep.append((d_input, d_output))
+        return idx.value
+
+    def commit(self) -> None:
+        check(lib().dd_batch_commit(self._h))
+
+    def run(self, stream=None, graph: bool = True) -> None:
+        check(lib().dd_batch_run(self._h, C.c_void_p(_stream(stream)), int(graph)))
+
+    def check(self, stream=None) -> None:
+        check(lib().dd_batch_check(self._h, C.c_void_p(_stream(stream))))
+
+    def info(self) -> dict:
+        p, t, g = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        check(lib().dd_batch_info(self._h, C.byref(p), C.byref(t), C.byref(g)))
+        return {"problems": p.value, "tiles": t.value, "grid": g.value}
+
+    def close(self) -> None:
+        if self._h:
+            lib().dd_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self) -> None:
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Plan:
     """Device-side plan of one mode: tables uploaded once, runs enqueued on a
     stream with device pointers (raw ints or tensors exposing data_ptr())."""

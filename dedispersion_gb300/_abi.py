@@ -124,6 +124,23 @@ SIGNATURES = {
     "dd_plan_launches": (C.c_int, [_P, _U32P]),
     "dd_plan_get_conf": (C.c_int, [_P, _CONF]),
     "dd_plan_destroy": (C.c_int, [_P]),
+    "dd_batch_create": (C.c_int, [C.POINTER(_P), C.c_int]),
+    "dd_batch_add": (C.c_int, [_P, _OBS, C.c_uint32, C.c_uint32, _F32P, _U32P, _U32P, _P, _P,
+                               _U32P]),
+    "dd_batch_commit": (C.c_int, [_P]),
+    "dd_batch_run": (C.c_int, [_P, _P, C.c_int]),
+    "dd_batch_check": (C.c_int, [_P, _P]),
+    "dd_batch_info": (C.c_int, [_P, _U32P, _U32P, _U32P]),
+    "dd_batch_destroy": (C.c_int, [_P]),
+    "dd_stream_bytes": (C.c_int, [_OBS, C.c_int, C.c_uint32, C.c_uint32, _F32P, _F32P, _U32P,
+                                  C.POINTER(C.c_uint64), _U32P]),
+    "dd_stream_create": (C.c_int, [C.POINTER(_P), _OBS, C.c_int, C.c_uint32, C.c_uint32, _F32P,
+                                   _F32P, _U32P, C.c_int]),
+    "dd_stream_buffers": (C.c_int, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),
+    "dd_stream_info": (C.c_int, [_P, _U32P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
+                                 _U32P]),
+    "dd_stream_push": (C.c_int, [_P, _P]),
+    "dd_stream_destroy": (C.c_int, [_P]),
 }
 
 _lib: C.CDLL | None = None

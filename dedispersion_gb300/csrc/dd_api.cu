@@ -435,6 +435,49 @@ dd_status rebuild(dd_plan *p) {
 namespace dd {
 // Lets other translation units of the library report through dd_last_error.
 void set_last_error(const char *message) { g_error = message; }
+
+// The kernel arguments of one run of `p` on the given device buffers; also
+// the rows each group sums (the cost of one of its tiles).
+dd_status plan_problem(const dd_plan *p, const void *d_input, float *d_output,
+                       ProblemDesc *out, uint64_t *rows_per_group) {
+  if (!p->ready)
+    return fail(DD_ERR_INVALID_ARGUMENT, p->have_shifts ? "plan tables are invalid: %s"
+                                                        : "plan has no shift table%s",
+                p->have_shifts ? g_error.c_str() : "");
+  const uint64_t tiles = (uint64_t)p->nr_groups * p->tiles_d * p->tiles_t;
+  if (tiles && (!d_input || !d_output)) return fail(DD_ERR_INVALID_ARGUMENT, "NULL data pointer");
+  if (tiles > 0x7fffffffull)
+    return fail(DD_ERR_UNSUPPORTED, "problem has %llu tiles", (unsigned long long)tiles);
+  const Dims &d = p->dims;
+  ProblemDesc P{};
+  P.in = static_cast<const uint8_t *>(d_input);
+  P.out = d_output;
+  P.groups = p->d_groups;
+  P.entries = p->d_entries;
+  P.status = p->d_status;
+  P.row_bytes = d.row_bytes;
+  P.out_dm_stride = p->out_dm_stride;
+  P.nr_groups = p->nr_groups;
+  P.nr_dms = d.nr_dms;
+  P.nr_samples = d.nr_samples;
+  P.bits = p->mode == DD_STEP_TWO ? 32 : p->bits;
+  P.first_dm = d.first_dm;
+  P.dm_step = d.dm_step;
+  P.win_samples = p->win;
+  P.tiles_t = p->tiles_t;
+  P.tiles_d = p->tiles_d;
+  P.tma = (d.row_bytes % 16 == 0 && reinterpret_cast<uintptr_t>(d_input) % 16 == 0) ? 1u : 0u;
+  P.out_vec4 = (d.out_row % 4 == 0 && reinterpret_cast<uintptr_t>(d_output) % 16 == 0) ? 1u : 0u;
+  P.mul_hi8 = 1u << 24;
+  if (p->use_delay_tables) {
+    P.delay_rows = (uint32_t)p->delay_shift.size();
+    P.delay_rel = p->d_delay_rel;
+  }
+  *out = P;
+  if (rows_per_group)
+    *rows_per_group = p->nr_groups ? p->entries.size() / p->nr_groups : 0;
+  return DD_OK;
+}
 }  // namespace dd
 
 extern "C" {
@@ -707,39 +750,11 @@ dd_status dd_plan_set_beam_mapping(dd_plan *p, const uint32_t *mapping, size_t n
 
 dd_status dd_plan_run(dd_plan *p, const void *d_input, float *d_output, void *stream) {
   if (!p) return fail(DD_ERR_INVALID_ARGUMENT, "plan is NULL");
-  if (!p->ready)
-    return fail(DD_ERR_INVALID_ARGUMENT, p->have_shifts ? "plan tables are invalid: %s"
-                                                        : "plan has no shift table%s",
-                p->have_shifts ? g_error.c_str() : "");
+  dd::ProblemDesc P{};
+  dd_status st = dd::plan_problem(p, d_input, d_output, &P, nullptr);
+  if (st) return st;
   const uint64_t tiles = (uint64_t)p->nr_groups * p->tiles_d * p->tiles_t;
   if (tiles == 0) return DD_OK;
-  if (!d_input || !d_output) return fail(DD_ERR_INVALID_ARGUMENT, "NULL data pointer");
-  if (tiles > 0x7fffffffull) return fail(DD_ERR_UNSUPPORTED, "problem has %llu tiles", (unsigned long long)tiles);
-  const Dims &d = p->dims;
-  dd::ProblemDesc P{};
-  P.in = static_cast<const uint8_t *>(d_input);
-  P.out = d_output;
-  P.groups = p->d_groups;
-  P.entries = p->d_entries;
-  P.status = p->d_status;
-  P.row_bytes = d.row_bytes;
-  P.out_dm_stride = p->out_dm_stride;
-  P.nr_groups = p->nr_groups;
-  P.nr_dms = d.nr_dms;
-  P.nr_samples = d.nr_samples;
-  P.bits = p->mode == DD_STEP_TWO ? 32 : p->bits;
-  P.first_dm = d.first_dm;
-  P.dm_step = d.dm_step;
-  P.win_samples = p->win;
-  P.tiles_t = p->tiles_t;
-  P.tiles_d = p->tiles_d;
-  P.tma = (d.row_bytes % 16 == 0 && reinterpret_cast<uintptr_t>(d_input) % 16 == 0) ? 1u : 0u;
-  P.out_vec4 = (d.out_row % 4 == 0 && reinterpret_cast<uintptr_t>(d_output) % 16 == 0) ? 1u : 0u;
-  P.mul_hi8 = 1u << 24;
-  if (p->use_delay_tables) {
-    P.delay_rows = (uint32_t)p->delay_shift.size();
-    P.delay_rel = p->d_delay_rel;
-  }
   DeviceGuard g(p->device);
   if (!g.ok) return fail(DD_ERR_CUDA, "cannot select device %d", p->device);
   p->kinfo->launch(P, (unsigned)tiles, p->smem, static_cast<cudaStream_t>(stream));

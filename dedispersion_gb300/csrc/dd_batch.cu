@@ -1,0 +1,333 @@
+// dd_batch.cu -- many single-step problems in one persistent launch.
+//
+// A batch holds any number of single-step problems of 1/2/4/8-bit input
+// (beams with their own channel count, sample count, DM range, DM step, input
+// width, zapped mask and device buffers).  Committing it lays all their tiles
+// out in one work list, longest tiles first (a tile's cost is its live rows),
+// and records a CUDA graph of [reset work counter, persistent kernel].  The
+// persistent kernel runs one CTA per free slot of every SM; each CTA takes the
+// next tile from the work counter and computes it with the same tile routine
+// as the plain kernel, so results equal the plain path's bit for bit.
+//
+// There is no counterpart in the reference (its test driver launches one
+// kernel per configuration and beam set, src/DedispersionTest.cpp:366-399).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "../../include/dedisp_gb300.h"
+#include "dd_device.cuh"
+
+namespace dd {
+void set_last_error(const char *message);
+// Plan internals shared with dd_api.cu.
+dd_status plan_problem(const dd_plan *plan, const void *d_input, float *d_output,
+                       ProblemDesc *problem, uint64_t *rows_per_group);
+}
+
+namespace {
+
+// The batch kernel's tile configuration: the engine's default swar8 tile.
+constexpr int kNW = 4, kNDT = 4, kTY = 8, kCH = 8;
+constexpr int kVar = dd::kUnpackPermuteMad;
+constexpr int kThreads = 32 * kTY;
+
+struct BatchDesc {
+  const dd::ProblemDesc *problems;  // sorted by tile cost, descending
+  const uint32_t *tile_start;       // prefix sums of tiles, nproblems + 1
+  uint32_t *counter;                // work counter (reset before each launch)
+  uint32_t nproblems;
+  uint32_t total_tiles;
+  dd::SmemLayout layout;            // uniform over the batch
+};
+
+__global__ void __launch_bounds__(kThreads, 2) batch_kernel(const BatchDesc B) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  __shared__ dd::ProblemDesc sP;
+  __shared__ uint32_t s_tile, s_local;
+  dd::init_barriers(smem, B.layout, kCH);
+  uint32_t sc = 0;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const uint32_t t = atomicAdd(B.counter, 1u);
+      s_tile = t;
+      if (t < B.total_tiles) {
+        uint32_t lo = 0, hi = B.nproblems;  // last p with tile_start[p] <= t
+        while (hi - lo > 1) {
+          const uint32_t mid = (lo + hi) / 2;
+          if (B.tile_start[mid] <= t) lo = mid; else hi = mid;
+        }
+        sP = B.problems[lo];
+        s_local = t - B.tile_start[lo];
+      }
+    }
+    __syncthreads();
+    if (s_tile >= B.total_tiles) break;
+    uint32_t g, dtile, ttile;
+    dd::decode_tile(sP, s_local, g, dtile, ttile);
+    // This problem's window and fetch size inside the batch's uniform slots.
+    dd::SmemLayout L = dd::make_layout(dd::kFamilySwar8, sP.win_samples, sP.bits, kCH, kTY * kNDT);
+    L.raw_stride = B.layout.raw_stride;
+    L.area_words = B.layout.area_words;
+    L.off_raw = B.layout.off_raw;
+    L.off_copy = B.layout.off_copy;
+    L.total = B.layout.total;
+    const bool ok = dd::swar8_tile<kNW, kNDT, kTY, kCH, kVar>(sP, sP.groups[g], dtile, ttile,
+                                                                 smem, L, sc);
+    if (!ok) break;  // uniform: decided by a block-wide vote inside the tile
+    __syncthreads();  // everyone is done with sP and s_tile
+  }
+}
+
+dd_status fail(dd_status code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  dd::set_last_error(buf);
+  return code;
+}
+
+dd_status cuda_fail(cudaError_t e, const char *what) {
+  (void)cudaGetLastError();
+  if (e == cudaErrorMemoryAllocation)
+    return fail(DD_ERR_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
+  return fail(DD_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define DDB_CUDA(call, what)                           \
+  do {                                                 \
+    cudaError_t e_ = (call);                           \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+}  // namespace
+
+struct dd_batch {
+  int device = 0;
+  std::vector<dd_plan *> plans;
+  std::vector<const void *> inputs;
+  std::vector<float *> outputs;
+  // committed state
+  bool committed = false;
+  dd::ProblemDesc *d_problems = nullptr;
+  uint32_t *d_tile_start = nullptr;
+  uint32_t *d_scratch = nullptr;  // [0] work counter, [1] status word
+  BatchDesc desc{};
+  size_t smem = 0;
+  unsigned grid = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t capture = nullptr;
+};
+
+namespace {
+
+void release(dd_batch *b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  if (b->capture) cudaStreamDestroy(b->capture);
+  if (b->d_problems) cudaFree(b->d_problems);
+  if (b->d_tile_start) cudaFree(b->d_tile_start);
+  if (b->d_scratch) cudaFree(b->d_scratch);
+  b->exec = nullptr; b->graph = nullptr; b->capture = nullptr;
+  b->d_problems = nullptr; b->d_tile_start = nullptr; b->d_scratch = nullptr;
+  b->committed = false;
+}
+
+// Enqueue [counter reset, kernel] on `s`.
+dd_status enqueue(dd_batch *b, cudaStream_t s) {
+  DDB_CUDA(cudaMemsetAsync(b->d_scratch, 0, sizeof(uint32_t), s), "reset work counter");
+  batch_kernel<<<b->grid, kThreads, b->smem, s>>>(b->desc);
+  DDB_CUDA(cudaGetLastError(), "launch batch kernel");
+  return DD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+dd_status dd_batch_create(dd_batch **batch, int device) {
+  if (!batch) return fail(DD_ERR_INVALID_ARGUMENT, "batch is NULL");
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    (void)cudaGetLastError();
+    return fail(DD_ERR_NO_DEVICE, "no CUDA device available");
+  }
+  if (device < 0 || device >= n) return fail(DD_ERR_INVALID_ARGUMENT, "device %d out of range", device);
+  *batch = new dd_batch();
+  (*batch)->device = device;
+  return DD_OK;
+}
+
+dd_status dd_batch_add(dd_batch *b, const dd_observation *obs, uint32_t input_bits,
+                       uint32_t padding, const float *shifts, const uint32_t *zapped,
+                       const uint32_t *beam_mapping, const void *d_input, float *d_output,
+                       uint32_t *index) {
+  if (!b || !obs || !shifts || !zapped || !beam_mapping || !d_input || !d_output)
+    return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (input_bits > 8) return fail(DD_ERR_UNSUPPORTED, "batches take 1/2/4/8-bit input");
+  dd_conf conf{0, 1, kCH, 32, kTY, 1, 4 * kNW, kNDT, 1};
+  dd_plan *p = nullptr;
+  dd_status st = dd_plan_create(&p, obs, DD_SINGLE_STEP, input_bits, padding, &conf, b->device);
+  if (st) return st;
+  dd_layout lay;
+  st = dd_get_layout(obs, DD_SINGLE_STEP, input_bits, padding, nullptr, &lay);
+  if (!st) st = dd_plan_set_shifts(p, shifts, obs->nr_channels);
+  if (!st) st = dd_plan_set_zapped(p, zapped, obs->nr_channels);
+  if (!st) st = dd_plan_set_beam_mapping(p, beam_mapping,
+                                         (size_t)obs->nr_synthesized_beams * lay.mapping_row_elems);
+  if (st) {
+    dd_plan_destroy(p);
+    return st;
+  }
+  if (b->committed) release(b);
+  if (index) *index = (uint32_t)b->plans.size();
+  b->plans.push_back(p);
+  b->inputs.push_back(d_input);
+  b->outputs.push_back(d_output);
+  return DD_OK;
+}
+
+dd_status dd_batch_commit(dd_batch *b) {
+  if (!b) return fail(DD_ERR_INVALID_ARGUMENT, "batch is NULL");
+  if (b->plans.empty()) return fail(DD_ERR_INVALID_ARGUMENT, "batch is empty");
+  release(b);
+  const size_t n = b->plans.size();
+  std::vector<dd::ProblemDesc> probs(n);
+  std::vector<uint64_t> rows(n);
+  for (size_t i = 0; i < n; i++) {
+    dd_status st = dd::plan_problem(b->plans[i], b->inputs[i], b->outputs[i], &probs[i], &rows[i]);
+    if (st) return st;
+  }
+  // Uniform slots sized for the largest raw row and copy of any problem; each
+  // tile fetches and builds only its own problem's window inside them.
+  dd::SmemLayout L{};
+  uint32_t raw_stride = 0, copy_words = 0;
+  for (auto &P : probs) {
+    const dd::SmemLayout l = dd::make_layout(dd::kFamilySwar8, P.win_samples, P.bits, kCH, kTY * kNDT);
+    raw_stride = std::max(raw_stride, l.raw_bytes);
+    copy_words = std::max(copy_words, l.copy_words);
+  }
+  L.raw_bytes = raw_stride;
+  L.raw_stride = raw_stride;
+  L.copy_words = copy_words;
+  L.area_words = kCH * 4u * copy_words;
+  L.off_bar = 0;
+  L.off_wstart = 64;
+  L.off_table = dd::round_up(L.off_wstart + 2u * dd::kNRaw * kCH * 4u, 128u);
+  L.off_raw = dd::round_up(L.off_table + 2u * kCH * kTY * kNDT * 4u, 128u);
+  L.off_copy = dd::round_up(L.off_raw + dd::kNRaw * kCH * L.raw_stride, 128u);
+  L.total = L.off_copy + 2u * L.area_words * 4u;
+  // Longest tiles first: a tile's cost is the rows its group sums.
+  std::vector<size_t> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](size_t x, size_t y) { return rows[x] > rows[y]; });
+  std::vector<dd::ProblemDesc> sorted(n);
+  std::vector<uint32_t> start(n + 1, 0);
+  uint64_t total = 0;
+  for (size_t k = 0; k < n; k++) {
+    sorted[k] = probs[order[k]];
+    start[k] = (uint32_t)total;
+    total += (uint64_t)sorted[k].nr_groups * sorted[k].tiles_d * sorted[k].tiles_t;
+  }
+  if (total > 0xffffffffull - 1) return fail(DD_ERR_UNSUPPORTED, "batch has too many tiles");
+  start[n] = (uint32_t)total;
+
+  int smem_max = 0, sms = 0, per_sm = 0;
+  DDB_CUDA(cudaSetDevice(b->device), "select device");
+  DDB_CUDA(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device),
+           "query shared memory");
+  DDB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device), "query SMs");
+  const size_t static_smem = sizeof(dd::ProblemDesc) + 64;
+  if (L.total + static_smem > (size_t)smem_max)
+    return fail(DD_ERR_UNSUPPORTED, "batch window needs %u bytes of shared memory", L.total);
+  DDB_CUDA(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                smem_max - (int)static_smem),
+           "set kernel shared memory");
+  DDB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, kThreads, L.total),
+           "occupancy");
+  if (per_sm < 1) return fail(DD_ERR_UNSUPPORTED, "batch kernel does not fit on an SM");
+  b->smem = L.total;
+  b->grid = (unsigned)std::min<uint64_t>((uint64_t)sms * per_sm, std::max<uint64_t>(1, total));
+
+  for (auto &P : sorted) P.status = nullptr;
+  DDB_CUDA(cudaMalloc(&b->d_problems, n * sizeof(dd::ProblemDesc)), "allocate problems");
+  DDB_CUDA(cudaMalloc(&b->d_tile_start, (n + 1) * sizeof(uint32_t)), "allocate tile table");
+  DDB_CUDA(cudaMalloc(&b->d_scratch, 2 * sizeof(uint32_t)), "allocate work counter");
+  for (auto &P : sorted) P.status = b->d_scratch + 1;
+  DDB_CUDA(cudaMemset(b->d_scratch, 0, 2 * sizeof(uint32_t)), "clear batch scratch");
+  DDB_CUDA(cudaMemcpy(b->d_problems, sorted.data(), n * sizeof(dd::ProblemDesc),
+                      cudaMemcpyHostToDevice), "upload problems");
+  DDB_CUDA(cudaMemcpy(b->d_tile_start, start.data(), (n + 1) * sizeof(uint32_t),
+                      cudaMemcpyHostToDevice), "upload tile table");
+  b->desc.problems = b->d_problems;
+  b->desc.tile_start = b->d_tile_start;
+  b->desc.counter = b->d_scratch;
+  b->desc.nproblems = (uint32_t)n;
+  b->desc.total_tiles = (uint32_t)total;
+  b->desc.layout = L;
+  // Record the launch as a graph: replays cost one graph launch.
+  DDB_CUDA(cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking), "create stream");
+  DDB_CUDA(cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal), "begin capture");
+  dd_status st = enqueue(b, b->capture);
+  cudaError_t e = cudaStreamEndCapture(b->capture, &b->graph);
+  if (st) return st;
+  if (e != cudaSuccess) return cuda_fail(e, "end capture");
+  DDB_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0), "instantiate graph");
+  b->committed = true;
+  return DD_OK;
+}
+
+dd_status dd_batch_run(dd_batch *b, void *stream, int use_graph) {
+  if (!b) return fail(DD_ERR_INVALID_ARGUMENT, "batch is NULL");
+  if (!b->committed) return fail(DD_ERR_INVALID_ARGUMENT, "batch is not committed");
+  DDB_CUDA(cudaSetDevice(b->device), "select device");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (use_graph) {
+    DDB_CUDA(cudaGraphLaunch(b->exec, s), "launch graph");
+    return DD_OK;
+  }
+  return enqueue(b, s);
+}
+
+dd_status dd_batch_check(dd_batch *b, void *stream) {
+  if (!b) return fail(DD_ERR_INVALID_ARGUMENT, "batch is NULL");
+  if (!b->committed) return fail(DD_ERR_INVALID_ARGUMENT, "batch is not committed");
+  DDB_CUDA(cudaSetDevice(b->device), "select device");
+  DDB_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)), "synchronize stream");
+  uint32_t status = 0;
+  DDB_CUDA(cudaMemcpy(&status, b->d_scratch + 1, sizeof(status), cudaMemcpyDeviceToHost),
+           "read status");
+  if (status) {
+    cudaMemset(b->d_scratch + 1, 0, sizeof(uint32_t));
+    return fail(DD_ERR_TIMEOUT, "a bounded wait for a staged row ran out on the device");
+  }
+  return DD_OK;
+}
+
+dd_status dd_batch_info(const dd_batch *b, uint32_t *problems, uint32_t *tiles, uint32_t *grid) {
+  if (!b) return fail(DD_ERR_INVALID_ARGUMENT, "batch is NULL");
+  if (problems) *problems = (uint32_t)b->plans.size();
+  if (tiles) *tiles = b->committed ? b->desc.total_tiles : 0;
+  if (grid) *grid = b->committed ? b->grid : 0;
+  return DD_OK;
+}
+
+dd_status dd_batch_destroy(dd_batch *b) {
+  if (!b) return DD_OK;
+  cudaSetDevice(b->device);
+  release(b);
+  for (dd_plan *p : b->plans) dd_plan_destroy(p);
+  delete b;
+  return DD_OK;
+}
+
+}  // extern "C"

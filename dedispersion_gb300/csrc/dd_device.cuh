@@ -53,8 +53,10 @@ __host__ __device__ inline uint32_t align_samples(uint32_t bits) {
 
 // Shared memory layout of one CTA (byte offsets from the dynamic base).
 struct SmemLayout {
-  uint32_t raw_bytes;   // one staged row in a raw slot
+  uint32_t raw_bytes;   // bytes fetched per staged row
+  uint32_t raw_stride;  // bytes between raw slots (>= raw_bytes)
   uint32_t copy_words;  // words of one shifted copy (swar8)
+  uint32_t area_words;  // words between copy areas (>= CH * 4 * copy_words)
   uint32_t off_bar, off_wstart, off_table, off_raw, off_copy, total;
 };
 
@@ -74,8 +76,10 @@ __host__ __device__ inline SmemLayout make_layout(int family, uint32_t win,
   L.off_wstart = 64;
   L.off_table = round_up(L.off_wstart + 2u * kNRaw * ch * 4u, 128u);
   L.off_raw = round_up(L.off_table + 2u * ch * tile_d * 4u, 128u);
-  L.off_copy = round_up(L.off_raw + kNRaw * ch * L.raw_bytes, 128u);
-  L.total = L.off_copy + 2u * ch * 4u * L.copy_words * 4u;
+  L.raw_stride = L.raw_bytes;
+  L.area_words = ch * 4u * L.copy_words;
+  L.off_copy = round_up(L.off_raw + kNRaw * ch * L.raw_stride, 128u);
+  L.total = L.off_copy + 2u * L.area_words * 4u;
   return L;
 }
 
@@ -184,7 +188,8 @@ struct StageCtx {
   uint32_t *wstart;  // first staged sample of each row of a slot
   uint32_t *wmod;    // t0 + delay(row, first DM of the tile) - wstart
   uint8_t *raw;
-  uint32_t raw_bytes;
+  uint32_t raw_bytes;   // fetched per row
+  uint32_t raw_stride;  // between slots
 };
 
 // Issue stage `s` (global stage index gs) of group G: lanes 0..CH-1 of the
@@ -220,7 +225,7 @@ __device__ __forceinline__ void issue_stage(const ProblemDesc &P,
     const uint32_t bytes =
         avail < S.raw_bytes ? static_cast<uint32_t>(avail) : S.raw_bytes;
     mbar_arrive_expect_tx(bar, bytes);
-    bulk_g2s(S.raw + (slot * CH + lane) * S.raw_bytes,
+    bulk_g2s(S.raw + (slot * CH + lane) * S.raw_stride,
              P.in + E.row_offset + boff, bytes, bar);
   } else {
     mbar_arrive(bar);
@@ -289,7 +294,7 @@ __device__ __forceinline__ void copy_stage_plain(const ProblemDesc &P,
     const uint64_t boff = P.bits <= 8 ? (uint64_t)ws * P.bits / 8u
                                       : (uint64_t)ws * (P.bits / 8u);
     const uint8_t *src = P.in + E.row_offset;
-    uint8_t *dst = S.raw + (slot * CH + ch) * S.raw_bytes;
+    uint8_t *dst = S.raw + (slot * CH + ch) * S.raw_stride;
     for (uint32_t b = tx; b < S.raw_bytes; b += 32)
       dst[b] = (boff + b < P.row_bytes) ? src[boff + b] : 0;
   }
@@ -365,6 +370,7 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
   S.wmod = S.wstart + kNRaw * CH;
   S.raw = smem + L.off_raw;
   S.raw_bytes = L.raw_bytes;
+  S.raw_stride = L.raw_stride;
   uint32_t *table = reinterpret_cast<uint32_t *>(smem + L.off_table);
   uint32_t *copies = reinterpret_cast<uint32_t *>(smem + L.off_copy);
 
@@ -421,9 +427,9 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
     }
     // Expand to bytes and write the four shifted copies of each row, two
     // words per thread and step (copy m word k = samples 4k+m .. 4k+m+3).
-    uint32_t *ac = copies + area * (CH * 4u * cw);
+    uint32_t *ac = copies + area * L.area_words;
     for (uint32_t ch = ty; ch < cnt; ch += TY) {
-      const uint8_t *r = S.raw + (slot * CH + ch) * S.raw_bytes;
+      const uint8_t *r = S.raw + (slot * CH + ch) * S.raw_stride;
       uint32_t *dst = ac + ch * 4u * cw;
       for (uint32_t k = 2 * tx; k < cw; k += 64) {
         uint32_t w0, w1, w2;
@@ -604,6 +610,7 @@ __device__ __forceinline__ bool scalar_tile(const ProblemDesc &P,
   S.wmod = S.wstart + kNRaw * CH;
   S.raw = smem + L.off_raw;
   S.raw_bytes = L.raw_bytes;
+  S.raw_stride = L.raw_stride;
   uint32_t *table = reinterpret_cast<uint32_t *>(smem + L.off_table);
   const uint32_t raws = smem_addr(S.raw) + (uint32_t)sizeof(T) * tx;
 
@@ -638,7 +645,7 @@ __device__ __forceinline__ bool scalar_tile(const ProblemDesc &P,
       if (idx < cnt * kTileD) {
         const uint32_t ch = idx / kTileD;
         const uint32_t o = delays.offset(P, G, S, r, s, slot, t0, d0);
-        tb[idx] = (slot * CH + ch) * L.raw_bytes + (uint32_t)sizeof(T) * o;
+        tb[idx] = (slot * CH + ch) * L.raw_stride + (uint32_t)sizeof(T) * o;
       }
     }
     if (s + 1 < nst)

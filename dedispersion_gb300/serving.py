@@ -1,0 +1,258 @@
+"""Real-time serving of many beams of batch streams.
+
+Each beam is a ``dd_stream`` (dedispersion_gb300/csrc/dd_stream.cu): device
+ring rows [max-delay tail | new batch], a pinned staging input and a pinned
+output, and one recorded CUDA graph per push (copy in, dedisperse -- single
+step, or step one then step two --, copy out, carry the tail).  The server:
+
+* admits beams against an HBM budget, from each stream's device bytes known
+  before it is created (``dd_stream_bytes``); a beam that does not fit is
+  refused with DD_ERR_OVER_BUDGET;
+* runs a schedule of batch arrivals (per beam a batch every period, delayed
+  by an exponential jitter -- Poisson-jittered arrivals), one CUDA stream per
+  beam so that beams overlap on the GPU, at most one batch in flight per beam
+  and later arrivals of a busy beam queued;
+* reports per-batch latency (arrival -> output in host memory), p50/p99
+  against the deadline (the batch period), and throughput in DM-samples/s.
+
+No counterpart in the reference: its streaming mode (splitBatches) was never
+implemented (include/Dedispersion.hpp:202; README.md:76-79).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import (DedispersionError, Observation, _abi, getShifts, getShiftsStepTwo)
+from ._abi import check, lib
+from . import synthetic as syn
+
+
+@dataclass
+class BeamConfig:
+    """One beam's stream: 2.048 s batches of 25000 samples at 81.92 us by default."""
+
+    name: str = "beam"
+    channels: int = 1536
+    min_freq: float = 1220.0
+    bandwidth: float = 0.1953125
+    sampling_time: float = 81.92e-6
+    samples: int = 25000
+    dms: int = 2048
+    dm_step: float = 0.2
+    first_dm: float = 0.0
+    bits: int = 8
+    subband: bool = False
+    subbands: int = 32
+    dms_per_subband_dm: int = 32   # step-two DMs per step-one DM (subband mode)
+    padding: int = 128
+    zap_fraction: float = 0.05
+    seed: int = 0
+
+    @property
+    def period(self) -> float:
+        return self.samples * self.sampling_time
+
+    def observation(self) -> Observation:
+        o = Observation()
+        o.setNrBeams(1)
+        o.setNrSynthesizedBeams(1)
+        o.setNrSamplesPerBatch(self.samples)
+        o.setSamplingTime(self.sampling_time)
+        if self.subband:
+            o.setFrequencyRange(self.subbands, self.channels, self.min_freq, self.bandwidth)
+            d2 = self.dms_per_subband_dm
+            if self.dms % d2:
+                raise ValueError("dms must be a multiple of dms_per_subband_dm")
+            o.setDMRange(self.dms // d2, self.first_dm, self.dm_step * d2, True)
+            o.setDMRange(d2, 0.0, self.dm_step)
+        else:
+            o.setFrequencyRange(1, self.channels, self.min_freq, self.bandwidth)
+            o.setDMRange(self.dms, self.first_dm, self.dm_step)
+        return o
+
+    def tables(self):
+        obs = self.observation()
+        shifts = getShifts(obs, self.padding)
+        shifts2 = getShiftsStepTwo(obs, self.padding) if self.subband else None
+        zapped = syn.zapped_mask(self.channels, self.zap_fraction, self.seed, self.padding)
+        return obs, shifts, shifts2, zapped
+
+
+def _f32p(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def stream_bytes(cfg: BeamConfig) -> tuple[int, int]:
+    """(device bytes, carried tail samples) of a beam's stream, without a device."""
+    obs, shifts, shifts2, zapped = cfg.tables()
+    nbytes, tail = C.c_uint64(0), C.c_uint32(0)
+    check(lib().dd_stream_bytes(C.byref(obs.c), int(cfg.subband), cfg.bits, cfg.padding,
+                                _f32p(shifts), _f32p(shifts2),
+                                zapped.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                C.byref(nbytes), C.byref(tail)))
+    return nbytes.value, tail.value
+
+
+class Stream:
+    """One beam's device stream (wraps dd_stream)."""
+
+    def __init__(self, cfg: BeamConfig, device: int = 0):
+        self.cfg = cfg
+        self.obs, self.shifts, self.shifts2, self.zapped = cfg.tables()
+        self._h = C.c_void_p()
+        check(lib().dd_stream_create(C.byref(self._h), C.byref(self.obs.c), int(cfg.subband),
+                                     cfg.bits, cfg.padding, _f32p(self.shifts),
+                                     _f32p(self.shifts2),
+                                     self.zapped.ctypes.data_as(C.POINTER(C.c_uint32)), device))
+        tail, nbytes = C.c_uint32(0), C.c_uint64(0)
+        row, rows = C.c_uint64(0), C.c_uint32(0)
+        check(lib().dd_stream_info(self._h, C.byref(tail), C.byref(nbytes), C.byref(row),
+                                   C.byref(rows)))
+        self.tail, self.device_bytes = tail.value, nbytes.value
+        self.input_row_bytes, self.output_rows = row.value, rows.value
+        h_in, h_out, d_out = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        check(lib().dd_stream_buffers(self._h, C.byref(h_in), C.byref(h_out), C.byref(d_out)))
+        n_in = cfg.channels * self.input_row_bytes
+        self.staging = np.ctypeslib.as_array(C.cast(h_in, C.POINTER(C.c_uint8)),
+                                             shape=(n_in,)).reshape(cfg.channels, -1)
+        self.output = np.ctypeslib.as_array(C.cast(h_out, C.POINTER(C.c_float)),
+                                            shape=(self.output_rows * cfg.samples,)
+                                            ).reshape(self.output_rows, cfg.samples)
+        self.dm_samples = self.output_rows * cfg.samples
+
+    def push(self, cuda_stream) -> None:
+        s = cuda_stream if isinstance(cuda_stream, int) else int(cuda_stream.cuda_stream)
+        check(lib().dd_stream_push(self._h, C.c_void_p(s)))
+
+    def close(self) -> None:
+        if self._h:
+            lib().dd_stream_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def poisson_schedule(beams: int, batches: int, period: float, jitter: float, seed: int):
+    """Arrivals (time, beam, batch): batch k of beam b at phase_b + k * period +
+    Exp(jitter), sorted by time."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for b in range(beams):
+        phase = float(rng.uniform(0.0, period))
+        for k in range(batches):
+            out.append((phase + k * period + float(rng.exponential(jitter)), b, k))
+    out.sort()
+    return out
+
+
+@dataclass
+class ServeReport:
+    latencies: list = field(default_factory=list)  # seconds, per batch
+    dm_samples: int = 0
+    wall: float = 0.0
+    deadline: float = 0.0
+    time_compression: float = 1.0
+
+    def summary(self) -> dict:
+        lat = np.array(self.latencies) if self.latencies else np.zeros(1)
+        return {"batches": len(self.latencies),
+                "p50_latency_s": float(np.percentile(lat, 50)),
+                "p99_latency_s": float(np.percentile(lat, 99)),
+                "max_latency_s": float(lat.max()),
+                "deadline_s": self.deadline,
+                "deadline_misses": int((lat > self.deadline).sum()),
+                "throughput_dm_samples_per_s": self.dm_samples / self.wall if self.wall else 0.0,
+                "wall_s": self.wall, "time_compression": self.time_compression}
+
+
+class Server:
+    """Admits beams against an HBM budget and serves their batch streams."""
+
+    def __init__(self, budget_bytes: int = 150 * 10**9, device: int = 0):
+        self.budget = int(budget_bytes)
+        self.device = device
+        self.used = 0
+        self.streams: list[Stream] = []
+
+    def admit(self, cfg: BeamConfig) -> Stream:
+        need, _ = stream_bytes(cfg)
+        if self.used + need > self.budget:
+            raise DedispersionError(_abi.DD_ERR_OVER_BUDGET,
+                                    f"beam {cfg.name} needs {need} device bytes, "
+                                    f"{self.budget - self.used} of the budget are left")
+        s = Stream(cfg, self.device)
+        self.used += s.device_bytes
+        self.streams.append(s)
+        return s
+
+    def close(self) -> None:
+        for s in self.streams:
+            s.close()
+        self.streams.clear()
+        self.used = 0
+
+    def serve(self, schedule, source, consumer=None, time_compression: float = 1.0,
+              deadline: float | None = None) -> ServeReport:
+        """Run `schedule` [(arrival s, beam, batch)].  source(beam, batch,
+        staging) fills a beam's pinned staging input; consumer(beam, batch,
+        output) sees each finished output (pinned host rows)."""
+        import torch
+        n = len(self.streams)
+        cuda_streams = [torch.cuda.Stream(device=self.device) for _ in range(n)]
+        pending = [[] for _ in range(n)]     # arrived, not yet dispatched: (t_arrival, batch)
+        inflight = [None] * n                # (event, t_arrival, batch)
+        report = ServeReport(deadline=deadline if deadline is not None
+                             else max(s.cfg.period for s in self.streams),
+                             time_compression=time_compression)
+        t0 = time.perf_counter()
+
+        def now():
+            return (time.perf_counter() - t0) * time_compression
+
+        def finish(b):
+            ev, ta, k = inflight[b]
+            done = now()
+            report.latencies.append((done - ta) / time_compression)
+            report.dm_samples += self.streams[b].dm_samples
+            inflight[b] = None
+            if consumer is not None:
+                consumer(b, k, self.streams[b].output)
+
+        def dispatch(b):
+            if inflight[b] is not None or not pending[b]:
+                return
+            ta, k = pending[b].pop(0)
+            source(b, k, self.streams[b].staging)
+            self.streams[b].push(cuda_streams[b])
+            ev = torch.cuda.Event()
+            ev.record(cuda_streams[b])
+            inflight[b] = (ev, ta, k)
+
+        def poll():
+            for b in range(n):
+                if inflight[b] is not None and inflight[b][0].query():
+                    finish(b)
+                    dispatch(b)
+
+        for ta, b, k in schedule:
+            while now() < ta:
+                poll()
+                time.sleep(0.0002)
+            pending[b].append((ta, k))
+            poll()
+            dispatch(b)
+        while any(x is not None for x in inflight) or any(pending):
+            poll()
+            for b in range(n):
+                dispatch(b)
+            time.sleep(0.0002)
+        report.wall = (time.perf_counter() - t0)
+        return report

@@ -204,6 +204,56 @@ def make_input(obs: Observation, bits: int, padding: int, seed: int, *, mode: in
     return out.reshape(-1)
 
 
+def batched_shapes(count: int = 40, seed: int = 2024) -> list[dict]:
+    """Uneven beams for one batched launch: channels in {384, 1536} over the
+    same 300 MHz band from 1220 MHz, samples uniform over 8192-32768 in steps of
+    1024, DMs uniform over 512-4096 in steps of 128, DM step uniform over
+    0.1-0.5, input bits in {2, 4, 8}; 81.92 us sampling."""
+    rng = np.random.default_rng(seed)
+    shapes = []
+    for i in range(count):
+        ch = int(rng.choice([384, 1536]))
+        shapes.append({
+            "channels": ch,
+            "bandwidth": 300.0 / ch,
+            "samples": int(rng.integers(8, 33)) * 1024,
+            "dms": int(rng.integers(4, 33)) * 128,
+            "dm_step": float(np.float32(rng.uniform(0.1, 0.5))),
+            "bits": int(rng.choice([2, 4, 8])),
+            "seed": seed * 1000 + i,
+        })
+    return shapes
+
+
+def shape_observation(shape: dict, padding: int) -> Observation:
+    return make_observation(shape["channels"], 1220.0, shape["bandwidth"], 81.92e-6,
+                            shape["samples"], shape["dms"], 0.0, shape["dm_step"],
+                            padding=padding)
+
+
+def device_uniform_input(torch, obs: Observation, bits: int, padding: int, seed: int):
+    """Seeded input on the GPU, uniform over the full bit range, packed
+    LSB-first for sub-byte widths, in the single-step row layout."""
+    lay = _layout(obs, DD_SINGLE_STEP, bits, padding)
+    C_, n = obs.getNrChannels(), obs.getNrSamplesPerDispersedBatch()
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    vals = torch.randint(0, 1 << bits, (C_, n), generator=g, device="cuda", dtype=torch.int32)
+    row = int(lay.input_row_bytes)
+    buf = torch.zeros((obs.getNrBeams() * C_, row), dtype=torch.uint8, device="cuda")
+    if bits == 8:
+        buf[:C_, :n] = vals.to(torch.uint8)
+    else:
+        per = 8 // bits
+        m = -(-n // per) * per
+        padded = torch.zeros((C_, m), dtype=torch.int32, device="cuda")
+        padded[:, :n] = vals
+        shifts = (torch.arange(per, device="cuda", dtype=torch.int32) * bits)
+        packed = (padded.view(C_, m // per, per) << shifts).sum(dim=2).to(torch.uint8)
+        buf[:C_, :m // per] = packed
+    return buf.view(-1)
+
+
 def output_buffer(obs: Observation, mode: int, padding: int, bits: int = 8) -> np.ndarray:
     lay = _layout(obs, mode, bits if mode != DD_STEP_TWO else 32, padding)
     return np.zeros(lay.output_bytes // 4, dtype=np.float32)

@@ -277,6 +277,65 @@ dd_status dd_plan_launches(const dd_plan *plan, uint32_t *launches);
 dd_status dd_plan_get_conf(const dd_plan *plan, dd_conf *conf);
 dd_status dd_plan_destroy(dd_plan *plan);
 
+/* ---- batches: many beams in one persistent launch ------------------------ */
+/* No counterpart in the reference (its driver launches one kernel per beam
+ * set, src/DedispersionTest.cpp:366-399).  A batch holds single-step problems
+ * of 1/2/4/8-bit input, each with its own geometry, tables and device
+ * buffers; committing it builds one work list over all their tiles (longest
+ * first) and records a CUDA graph of [reset work counter, persistent kernel].
+ * Results equal dd_plan_run's for each problem bit for bit. */
+typedef struct dd_batch dd_batch;
+dd_status dd_batch_create(dd_batch **batch, int device);
+/* Add one single-step problem; `index` (may be NULL) receives its position.
+ * Host tables as for dd_dedispersion, device buffers as for dd_plan_run. */
+dd_status dd_batch_add(dd_batch *batch, const dd_observation *obs,
+                       uint32_t input_bits, uint32_t padding,
+                       const float *shifts, const uint32_t *zapped,
+                       const uint32_t *beam_mapping, const void *d_input,
+                       float *d_output, uint32_t *index);
+dd_status dd_batch_commit(dd_batch *batch);
+/* Enqueue the batch on `stream`: replay the recorded graph (use_graph = 1)
+ * or launch directly. */
+dd_status dd_batch_run(dd_batch *batch, void *stream, int use_graph);
+/* Synchronize `stream` and report a device-side timeout. */
+dd_status dd_batch_check(dd_batch *batch, void *stream);
+/* Problems, tiles and persistent CTAs of a committed batch. */
+dd_status dd_batch_info(const dd_batch *batch, uint32_t *problems,
+                        uint32_t *tiles, uint32_t *grid);
+dd_status dd_batch_destroy(dd_batch *batch);
+
+/* ---- streams: one beam of a real-time batch stream ---------------------- */
+/* No counterpart in the reference (its splitBatches mode is empty,
+ * include/Dedispersion.hpp:202).  `obs` gives the per-batch geometry: S new
+ * samples per batch (nr_samples_per_batch), one beam, the DM range(s) and, with
+ * `subband` = 1, the subband fields of a step one -> step two pipeline.  The
+ * stream keeps the max-delay tail of every channel on the device and each
+ * push dedisperses [tail | new batch]: output k equals the plain path on
+ * stream samples [k*S - tail, (k+1)*S) (zeros before the first batch). */
+typedef struct dd_stream dd_stream;
+/* Device bytes a stream of this geometry holds (for admission), and its tail. */
+dd_status dd_stream_bytes(const dd_observation *obs, int subband,
+                          uint32_t input_bits, uint32_t padding,
+                          const float *shifts, const float *shifts_step_two,
+                          const uint32_t *zapped, uint64_t *device_bytes,
+                          uint32_t *tail);
+dd_status dd_stream_create(dd_stream **stream, const dd_observation *obs,
+                           int subband, uint32_t input_bits, uint32_t padding,
+                           const float *shifts, const float *shifts_step_two,
+                           const uint32_t *zapped, int device);
+/* Pinned staging input [C][S samples], pinned output [rows][S], device
+ * output in the plan layout. */
+dd_status dd_stream_buffers(dd_stream *stream, void **h_input, float **h_output,
+                            float **d_output);
+dd_status dd_stream_info(const dd_stream *stream, uint32_t *tail,
+                         uint64_t *device_bytes, uint64_t *input_row_bytes,
+                         uint32_t *output_rows);
+/* Enqueue one batch (the staging input) on `cuda_stream`: copy in, dedisperse,
+ * copy the output to the pinned output, carry the tail.  Refill the staging
+ * input only after the previous push completed. */
+dd_status dd_stream_push(dd_stream *stream, void *cuda_stream);
+dd_status dd_stream_destroy(dd_stream *stream);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

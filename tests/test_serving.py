@@ -1,0 +1,123 @@
+"""Real-time serving: admission by device-memory budget, and every served
+batch equal to the plain path on its window [tail | batch]."""
+import numpy as np
+import pytest
+
+import dedispersion_gb300 as dd
+from dedispersion_gb300 import _abi, serving
+from dedispersion_gb300 import synthetic as syn
+
+
+def small_beams():
+    return [
+        serving.BeamConfig(name="single8", channels=256, bandwidth=0.5, samples=4096, dms=128,
+                           dm_step=0.2, bits=8, seed=1),
+        serving.BeamConfig(name="subband8", channels=256, bandwidth=0.5, samples=4096, dms=128,
+                           dm_step=0.2, bits=8, subband=True, subbands=16, dms_per_subband_dm=16,
+                           seed=2),
+        serving.BeamConfig(name="single4", channels=192, bandwidth=0.75, samples=2048, dms=96,
+                           dm_step=0.3, bits=4, seed=3),
+    ]
+
+
+def test_stream_bytes_and_admission_refusal(engine):
+    cfg = small_beams()[0]
+    nbytes, tail = serving.stream_bytes(cfg)
+    obs, shifts, _, zapped = cfg.tables()
+    lay = dd.layout(obs, dd.DD_SINGLE_STEP, 8, cfg.padding, shifts)
+    assert tail >= lay.max_delay and tail <= cfg.samples
+    ring = cfg.channels * dd.pad(cfg.samples + tail, cfg.padding)
+    out = cfg.dms * dd.pad(cfg.samples, cfg.padding // 4) * 4
+    assert nbytes == ring + out
+    sub = small_beams()[1]
+    nb2, _ = serving.stream_bytes(sub)
+    assert nb2 > 0
+    server = serving.Server(budget_bytes=nbytes - 1)
+    with pytest.raises(dd.DedispersionError) as e:
+        server.admit(cfg)
+    assert e.value.status == _abi.DD_ERR_OVER_BUDGET
+    assert server.used == 0 and not server.streams
+
+
+def batch_data(cfg, k):
+    rng = np.random.default_rng(1000 * cfg.seed + k)
+    vals = rng.integers(0, 1 << cfg.bits, size=(cfg.channels, cfg.samples), dtype=np.uint16)
+    if cfg.bits == 8:
+        return vals.astype(np.uint8)
+    return syn.pack_subbyte(vals.astype(np.uint8), cfg.bits, cfg.samples * cfg.bits // 8)
+
+
+def plain_reference(stream, window):
+    """The plain path (synchronous C ABI calls) on one [tail | batch] window."""
+    cfg = stream.cfg
+    obs = stream.obs.copy()
+    S = cfg.samples
+    if not cfg.subband:
+        obs.setNrSamplesPerDispersedBatch(S + stream.tail)
+        lay = dd.layout(obs, dd.DD_SINGLE_STEP, cfg.bits, cfg.padding)
+        inp = np.zeros((cfg.channels, lay.input_row_bytes), np.uint8)
+        inp[:, :window.shape[1]] = window
+        out = np.zeros(lay.output_bytes // 4, np.float32)
+        mapping = np.zeros(lay.mapping_row_elems, np.uint32)
+        dd.dedispersion(obs, stream.zapped, mapping, inp.reshape(-1), out, stream.shifts,
+                        cfg.padding, cfg.bits)
+        return out.reshape(-1, lay.output_row_elems)[:, :S]
+    s1 = S + serving_tail_step_two(stream)
+    obs.setNrSamplesPerBatch(s1, True)
+    obs.setNrSamplesPerDispersedBatch(S + stream.tail, True)
+    lay1 = dd.layout(obs, dd.DD_STEP_ONE, cfg.bits, cfg.padding)
+    inp = np.zeros((cfg.channels, lay1.input_row_bytes), np.uint8)
+    inp[:, :window.shape[1]] = window
+    mid = np.zeros(lay1.output_bytes // 4, np.float32)
+    dd.subbandDedispersionStepOne(obs, stream.zapped, inp.reshape(-1), mid, stream.shifts,
+                                  cfg.padding, cfg.bits)
+    lay2 = dd.layout(obs, dd.DD_STEP_TWO, 32, cfg.padding)
+    out = np.zeros(lay2.output_bytes // 4, np.float32)
+    mapping = np.zeros(lay2.mapping_row_elems, np.uint32)
+    dd.subbandDedispersionStepTwo(obs, mapping, mid, out, stream.shifts2, cfg.padding)
+    return out.reshape(-1, lay2.output_row_elems)[:, :S]
+
+
+def serving_tail_step_two(stream):
+    """Step-two max delay (S1 - S) of a subband stream."""
+    lay = dd.layout(stream.obs, dd.DD_STEP_TWO, 32, stream.cfg.padding, stream.shifts2)
+    return lay.max_delay
+
+
+@pytest.mark.gpu
+def test_served_batches_equal_plain_path(gpu):
+    pytest.importorskip("torch")
+    server = serving.Server(budget_bytes=150 * 10**9)
+    beams = small_beams()
+    for cfg in beams:
+        server.admit(cfg)
+    nb = 4
+    inputs = {}
+    outputs = {}
+
+    def source(b, k, staging):
+        data = batch_data(beams[b], k)
+        staging[:, :data.shape[1]] = data
+        inputs[(b, k)] = data
+
+    def consumer(b, k, out):
+        outputs[(b, k)] = out.copy()
+
+    schedule = serving.poisson_schedule(len(beams), nb, period=0.05, jitter=0.01, seed=5)
+    report = server.serve(schedule, source, consumer, time_compression=1.0, deadline=2.048)
+    s = report.summary()
+    assert s["batches"] == len(beams) * nb
+    assert s["p99_latency_s"] < 2.048
+    for b, stream in enumerate(server.streams):
+        cfg = stream.cfg
+        per = 8 // cfg.bits if cfg.bits < 8 else 1
+        tail_b = stream.tail // per
+        prev = np.zeros((cfg.channels, tail_b), np.uint8)
+        for k in range(nb):
+            cur = inputs[(b, k)]
+            window = np.concatenate([prev, cur], axis=1)
+            want = plain_reference(stream, window)
+            got = outputs[(b, k)]
+            assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (cfg.name, k)
+            prev = window[:, window.shape[1] - tail_b:] if tail_b else prev
+    server.close()
