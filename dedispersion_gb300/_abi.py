@@ -141,6 +141,16 @@ SIGNATURES = {
                                  _U32P]),
     "dd_stream_push": (C.c_int, [_P, _P]),
     "dd_stream_destroy": (C.c_int, [_P]),
+    "dd_mlp_create": (C.c_int, [C.POINTER(_P), C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64,
+                                C.c_int]),
+    "dd_mlp_param_count": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    "dd_mlp_get_params": (C.c_int, [_P, _F32P, C.c_uint64]),
+    "dd_mlp_set_params": (C.c_int, [_P, _F32P, C.c_uint64]),
+    "dd_mlp_forward": (C.c_int, [_P, _F32P, C.c_uint32, _F32P]),
+    "dd_mlp_gradients": (C.c_int, [_P, _F32P, _F32P, C.c_uint32, _F32P, _F32P]),
+    "dd_mlp_train": (C.c_int, [_P, _F32P, _F32P, C.c_uint32, C.c_uint32, C.c_float, _F32P]),
+    "dd_mlp_destroy": (C.c_int, [_P]),
+    "dd_plan_time": (C.c_int, [_P, _P, _P, C.c_uint32, C.c_uint32, _F32P, _F32P]),
 }
 
 _lib: C.CDLL | None = None

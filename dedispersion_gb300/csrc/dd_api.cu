@@ -243,6 +243,7 @@ struct dd_plan {
   uint16_t *d_delay_rel = nullptr;
   size_t cap_delay_rel = 0;
   bool use_delay_tables = false;
+  std::string invalid;  // why the tables are not usable (empty when ready)
   bool ready = false;
 };
 
@@ -443,7 +444,7 @@ dd_status plan_problem(const dd_plan *p, const void *d_input, float *d_output,
   if (!p->ready)
     return fail(DD_ERR_INVALID_ARGUMENT, p->have_shifts ? "plan tables are invalid: %s"
                                                         : "plan has no shift table%s",
-                p->have_shifts ? g_error.c_str() : "");
+                p->have_shifts ? p->invalid.c_str() : "");
   const uint64_t tiles = (uint64_t)p->nr_groups * p->tiles_d * p->tiles_t;
   if (tiles && (!d_input || !d_output)) return fail(DD_ERR_INVALID_ARGUMENT, "NULL data pointer");
   if (tiles > 0x7fffffffull)
@@ -721,13 +722,28 @@ dd_status dd_plan_create_with_kernel(dd_plan **plan, const dd_observation *o, dd
   return DD_OK;
 }
 
+namespace {
+// Rebuild after a table change.  Tables set one at a time can be
+// inconsistent in between (delays checked before the zapped mask arrives):
+// such errors are kept and reported by the next run; device errors return.
+dd_status rebuild_deferred(dd_plan *p) {
+  dd_status st = rebuild(p);
+  if (st == DD_ERR_INVALID_ARGUMENT || st == DD_ERR_UNSUPPORTED) {
+    p->invalid = g_error;
+    return DD_OK;
+  }
+  if (!st) p->invalid.clear();
+  return st;
+}
+}  // namespace
+
 dd_status dd_plan_set_shifts(dd_plan *p, const float *shifts, size_t n) {
   if (!p || !shifts) return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
   size_t need = p->mode == DD_STEP_TWO ? p->obs.nr_subbands : p->obs.nr_channels;
   if (n < need) return fail(DD_ERR_INVALID_ARGUMENT, "shift table has %zu entries, needs %zu", n, need);
   p->shifts.assign(shifts, shifts + need);
   p->have_shifts = true;
-  return rebuild(p);
+  return rebuild_deferred(p);
 }
 
 dd_status dd_plan_set_zapped(dd_plan *p, const uint32_t *zapped, size_t n) {
@@ -736,7 +752,7 @@ dd_status dd_plan_set_zapped(dd_plan *p, const uint32_t *zapped, size_t n) {
   if (n < p->obs.nr_channels)
     return fail(DD_ERR_INVALID_ARGUMENT, "zapped mask has %zu entries, needs %u", n, p->obs.nr_channels);
   p->zapped.assign(zapped, zapped + p->obs.nr_channels);
-  return rebuild(p);
+  return rebuild_deferred(p);
 }
 
 dd_status dd_plan_set_beam_mapping(dd_plan *p, const uint32_t *mapping, size_t n) {
@@ -745,7 +761,7 @@ dd_status dd_plan_set_beam_mapping(dd_plan *p, const uint32_t *mapping, size_t n
   size_t need = (size_t)p->obs.nr_synthesized_beams * p->dims.mapping_row;
   if (n < need) return fail(DD_ERR_INVALID_ARGUMENT, "beam mapping has %zu entries, needs %zu", n, need);
   p->mapping.assign(mapping, mapping + need);
-  return rebuild(p);
+  return rebuild_deferred(p);
 }
 
 dd_status dd_plan_run(dd_plan *p, const void *d_input, float *d_output, void *stream) {
@@ -775,6 +791,42 @@ dd_status dd_plan_check(dd_plan *p, void *stream) {
     return fail(DD_ERR_CUDA, "device status 0x%x", status);
   }
   return DD_OK;
+}
+
+dd_status dd_plan_time(dd_plan *p, const void *d_input, float *d_output, uint32_t warmup,
+                       uint32_t iterations, float *mean_ms, float *std_ms) {
+  if (!p || !mean_ms || iterations == 0) return fail(DD_ERR_INVALID_ARGUMENT, "bad argument");
+  DeviceGuard g(p->device);
+  cudaStream_t s = nullptr;
+  DD_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "create stream");
+  std::vector<cudaEvent_t> ev(iterations + 1, nullptr);
+  dd_status st = DD_OK;
+  for (auto &e : ev)
+    if (cudaEventCreate(&e) != cudaSuccess) st = cuda_fail(cudaGetLastError(), "create event");
+  for (uint32_t i = 0; i < warmup && !st; i++) st = dd_plan_run(p, d_input, d_output, s);
+  if (!st && cudaEventRecord(ev[0], s) != cudaSuccess) st = cuda_fail(cudaGetLastError(), "record");
+  for (uint32_t i = 0; i < iterations && !st; i++) {
+    st = dd_plan_run(p, d_input, d_output, s);
+    if (!st && cudaEventRecord(ev[i + 1], s) != cudaSuccess)
+      st = cuda_fail(cudaGetLastError(), "record");
+  }
+  if (!st) st = dd_plan_check(p, s);
+  if (!st) {
+    double sum = 0, sq = 0;
+    for (uint32_t i = 0; i < iterations; i++) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, ev[i], ev[i + 1]);
+      sum += ms;
+      sq += (double)ms * ms;
+    }
+    const double mean = sum / iterations;
+    *mean_ms = (float)mean;
+    if (std_ms) *std_ms = (float)std::sqrt(std::max(0.0, sq / iterations - mean * mean));
+  }
+  for (auto &e : ev)
+    if (e) cudaEventDestroy(e);
+  cudaStreamDestroy(s);
+  return st;
 }
 
 dd_status dd_plan_launches(const dd_plan *p, uint32_t *launches) {

@@ -1,0 +1,66 @@
+// dd_kernels.cuh -- kernel templates, launchers and registry-entry macros of
+// the compiled tile configurations (instantiated in dd_kernels_*.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "dd_device.cuh"
+
+namespace dd {
+
+
+// Grid-mapped kernel: one CTA per tile.
+template <int NW, int NDT, int TY, int CH, int VAR>
+__global__ void __launch_bounds__(32 * TY, (TY >= 16 ? 1 : (TY >= 8 ? 2 : 4)))
+    swar8_kernel(const ProblemDesc P) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  const SmemLayout L = make_layout(kFamilySwar8, P.win_samples, P.bits, CH, TY * NDT);
+  init_barriers(smem, L, CH);
+  uint32_t g, dtile, ttile, sc = 0;
+  decode_tile(P, blockIdx.x, g, dtile, ttile);
+  (void)swar8_tile<NW, NDT, TY, CH, VAR>(P, P.groups[g], dtile, ttile, smem, L, sc);
+}
+
+template <typename T, int NS, int NDT, int TY, int CH>
+__global__ void __launch_bounds__(32 * TY, (TY >= 8 ? 2 : 4))
+    scalar_kernel(const ProblemDesc P) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  const SmemLayout L = make_layout(kFamilyScalar, P.win_samples, P.bits, CH, TY * NDT);
+  init_barriers(smem, L, CH);
+  uint32_t g, dtile, ttile, sc = 0;
+  decode_tile(P, blockIdx.x, g, dtile, ttile);
+  (void)scalar_tile<T, NS, NDT, TY, CH>(P, P.groups[g], dtile, ttile, smem, L, sc);
+}
+
+template <int NW, int NDT, int TY, int CH, int VAR>
+void launch_swar8(const ProblemDesc &P, unsigned grid, size_t smem,
+                  cudaStream_t stream) {
+  swar8_kernel<NW, NDT, TY, CH, VAR><<<grid, 32 * TY, smem, stream>>>(P);
+}
+
+template <typename T, int NS, int NDT, int TY, int CH>
+void launch_scalar(const ProblemDesc &P, unsigned grid, size_t smem,
+                   cudaStream_t stream) {
+  scalar_kernel<T, NS, NDT, TY, CH><<<grid, 32 * TY, smem, stream>>>(P);
+}
+
+#define DD_SWAR8(NW, NDT, TY, CH, VAR)                                        \
+  {"swar8_i" #NW "_d" #NDT "_w" #TY "_c" #CH "_v" #VAR, kFamilySwar8, 8,     \
+   4 * NW, NDT, TY, CH, 32 * TY, 128 * NW, TY * NDT, VAR,                    \
+   reinterpret_cast<const void *>(&swar8_kernel<NW, NDT, TY, CH, VAR>),      \
+   &launch_swar8<NW, NDT, TY, CH, VAR>}
+
+#define DD_SCALAR(T, BITS, NS, NDT, TY, CH)                                   \
+  {"scalar" #BITS "_i" #NS "_d" #NDT "_w" #TY "_c" #CH, kFamilyScalar, BITS, \
+   NS, NDT, TY, CH, 32 * TY, 32 * NS, TY * NDT, 0,                            \
+   reinterpret_cast<const void *>(&scalar_kernel<T, NS, NDT, TY, CH>),       \
+   &launch_scalar<T, NS, NDT, TY, CH>}
+
+
+// Parts of the registry, one per translation unit (compiled in parallel).
+const KernelInfo *kernels_swar8_a(int *count);
+const KernelInfo *kernels_swar8_b(int *count);
+const KernelInfo *kernels_swar8_c(int *count);
+const KernelInfo *kernels_scalar(int *count);
+
+}  // namespace dd

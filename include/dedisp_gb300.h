@@ -336,6 +336,37 @@ dd_status dd_stream_info(const dd_stream *stream, uint32_t *tail,
 dd_status dd_stream_push(dd_stream *stream, void *cuda_stream);
 dd_status dd_stream_destroy(dd_stream *stream);
 
+/* ---- learned tuning: the cost model's network ---------------------------- */
+/* No counterpart in the reference (its tuner is an exhaustive sweep,
+ * src/DedispersionTuning.cpp:201-437, which stays the judge).  An MLP
+ * in -> hidden x hidden_layers -> 1 with ReLU, bf16 weights (fp32 master copy
+ * for Adam), fp32 accumulation, MSE loss, trained and run by the library's own
+ * CUDA kernels.  Parameters are exchanged as flat fp32 arrays: per layer
+ * W [out][in] then b [out]. */
+typedef struct dd_mlp dd_mlp;
+dd_status dd_mlp_create(dd_mlp **mlp, uint32_t in_features, uint32_t hidden,
+                        uint32_t hidden_layers, uint64_t seed, int device);
+dd_status dd_mlp_param_count(const dd_mlp *mlp, uint64_t *count);
+dd_status dd_mlp_get_params(dd_mlp *mlp, float *params, uint64_t count);
+dd_status dd_mlp_set_params(dd_mlp *mlp, const float *params, uint64_t count);
+/* Predictions for `n` rows of features (host arrays). */
+dd_status dd_mlp_forward(dd_mlp *mlp, const float *x, uint32_t n, float *y);
+/* MSE loss and its gradient w.r.t. every parameter (host arrays). */
+dd_status dd_mlp_gradients(dd_mlp *mlp, const float *x, const float *target,
+                           uint32_t n, float *grad, float *loss);
+/* `steps` full-batch Adam steps at learning rate `lr`; final loss out. */
+dd_status dd_mlp_train(dd_mlp *mlp, const float *x, const float *target,
+                       uint32_t n, uint32_t steps, float lr, float *final_loss);
+dd_status dd_mlp_destroy(dd_mlp *mlp);
+
+/* ---- tuning support ------------------------------------------------------ */
+/* Mean device time of `iterations` runs of a plan after `warmup` runs, timed
+ * with CUDA events on a private stream (the reference's tuner times
+ * enqueue + wait with a host timer, src/DedispersionTuning.cpp:384-395). */
+dd_status dd_plan_time(dd_plan *plan, const void *d_input, float *d_output,
+                       uint32_t warmup, uint32_t iterations, float *mean_ms,
+                       float *std_ms);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif
