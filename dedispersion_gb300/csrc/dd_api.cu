@@ -362,17 +362,25 @@ dd_status rebuild(dd_plan *p) {
   p->use_delay_tables = spread < 65536 && rows > 0 && p->tiles_d > 0;
   if (p->use_delay_tables) {
     p->delay_rel.assign((size_t)p->tiles_d * rows * k.tile_d, 0);
-    for (uint32_t t = 0; t < p->tiles_d; t++)
+    // DM values in the reference's order (firstDM + dm * dmStep, each op
+    // rounded to float: this file is compiled with -ffp-contract=off), then
+    // one product and truncation per entry; equal to dd::host_delay.
+    std::vector<float> dm_value((size_t)p->tiles_d * k.tile_d);
+    for (size_t i = 0; i < dm_value.size(); i++) {
+      const uint32_t dm = std::min((uint32_t)i, d.nr_dms - 1);
+      const float step_dm = static_cast<float>(dm) * d.dm_step;
+      dm_value[i] = d.first_dm + step_dm;
+    }
+    for (uint32_t t = 0; t < p->tiles_d; t++) {
+      const float *dv = &dm_value[(size_t)t * k.tile_d];
       for (size_t r = 0; r < rows; r++) {
         const float sh = p->delay_shift[r];
-        const uint32_t d0 = t * k.tile_d;
-        const uint32_t base = dd::host_delay(d.first_dm, d.dm_step, d0, sh);
+        const uint32_t base = static_cast<uint32_t>(dv[0] * sh);
         uint16_t *rel = &p->delay_rel[((size_t)t * rows + r) * k.tile_d];
-        for (int j = 0; j < k.tile_d; j++) {
-          const uint32_t dm = std::min(d0 + (uint32_t)j, d.nr_dms - 1);
-          rel[j] = (uint16_t)(dd::host_delay(d.first_dm, d.dm_step, dm, sh) - base);
-        }
+        for (int j = 0; j < k.tile_d; j++)
+          rel[j] = (uint16_t)(static_cast<uint32_t>(dv[j] * sh) - base);
       }
+    }
   }
   const uint32_t bits = family_bits(p->mode, p->bits) == 8 ? p->bits : family_bits(p->mode, p->bits);
   const uint32_t a = dd::window_alignment_samples(bits);

@@ -1,0 +1,442 @@
+"""Autotuning of the tile configuration: an exhaustive sweep and a learned
+cost model that times only its top candidates.
+
+* :func:`sweep` is the engine's DedispersionTuning (src/DedispersionTuning.cpp):
+  every compiled configuration of the input width's kernel family is run on
+  the problem and timed with CUDA events inside the library (dd_plan_time);
+  results carry the reference's GFLOP/s figure, 1e-9 * beams * DMs *
+  (channels - zapped) * samples / time (src/DedispersionTuning.cpp:327,
+  412-425).  ``python -m dedispersion_gb300.tuning`` takes the reference's
+  switches and prints its row format, or with -best the tuned-conf line
+  "nrDMs split local unroll tD0 tD1 tD2 iD0 iD1 iD2" (:416-437), which
+  readTunedDedispersionConf reads.
+* :class:`LearnedTuner` predicts log(time per DM-sample) of every configuration
+  from shape and configuration features with the library's CUDA MLP
+  (dedispersion_gb300.costmodel), then times only the top k.  The sweep stays
+  the judge; the model never touches outputs.
+"""
+from __future__ import annotations
+
+import argparse
+import math
+import sys
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import (DD_SINGLE_STEP, DD_STEP_ONE, DD_STEP_TWO, DedispersionConf, Plan, getShifts,
+               kernels, layout)
+from . import synthetic as syn
+from ._abi import check, lib
+
+import ctypes as C
+
+
+# ---------------------------------------------------------------------------
+# exhaustive sweep
+
+@dataclass
+class TuneResult:
+    kernel: int
+    name: str
+    conf: DedispersionConf
+    mean_ms: float
+    std_ms: float
+    gflops: float
+    wall_s: float  # tuning wall time spent on this configuration
+
+
+def family_kernels(mode: int, bits: int):
+    fam = 32 if mode == DD_STEP_TWO else (8 if bits <= 8 else bits)
+    return [k for k in kernels() if k.elem_bits == fam]
+
+
+def _time_plan(plan: Plan, d_in, d_out, warmup: int, iterations: int):
+    mean, std = C.c_float(0), C.c_float(0)
+    check(lib().dd_plan_time(plan._h, C.c_void_p(int(d_in.data_ptr())),
+                             C.c_void_p(int(d_out.data_ptr())), warmup, iterations,
+                             C.byref(mean), C.byref(std)))
+    return mean.value, std.value
+
+
+def work_units(obs, mode: int, live: int) -> float:
+    """beams x DMs x live rows x samples: the reference tuner's FLOP count."""
+    if mode == DD_SINGLE_STEP:
+        return obs.getNrSynthesizedBeams() * obs.getNrDMs() * live * obs.getNrSamplesPerBatch()
+    if mode == DD_STEP_ONE:
+        return obs.getNrBeams() * obs.getNrDMs(True) * live * obs.getNrSamplesPerBatch(True)
+    return (obs.getNrSynthesizedBeams() * obs.getNrDMs(True) * obs.getNrDMs() *
+            obs.getNrSubbands() * obs.getNrSamplesPerBatch())
+
+
+def sweep(obs, mode: int, bits: int, padding: int, shifts, zapped=None, mapping=None,
+          d_in=None, d_out=None, warmup: int = 1, iterations: int = 3, device: int = 0,
+          candidates=None) -> list[TuneResult]:
+    """Time every configuration in `candidates` (default: the whole family)."""
+    import torch
+    lay = layout(obs, mode, bits if mode != DD_STEP_TWO else 32, padding)
+    if d_in is None:
+        d_in = torch.randint(0, 255, (lay.input_bytes,), dtype=torch.uint8,
+                             device=f"cuda:{device}")
+        if mode == DD_STEP_TWO or bits == 32:
+            d_in = torch.rand(lay.input_bytes // 4, device=f"cuda:{device}")
+    if d_out is None:
+        d_out = torch.empty(lay.output_bytes // 4, dtype=torch.float32, device=f"cuda:{device}")
+    n = obs.getNrChannels() if mode != DD_STEP_TWO else obs.getNrSubbands()
+    live = n if zapped is None else int((np.asarray(zapped)[:n] == 0).sum())
+    units = work_units(obs, mode, live)
+    out = []
+    from . import DedispersionError
+    from ._abi import DD_ERR_INVALID_ARGUMENT, DD_ERR_UNSUPPORTED
+    for k in (candidates if candidates is not None else family_kernels(mode, bits)):
+        t0 = time.perf_counter()
+        plan = Plan(obs, mode, bits, padding, device=device, kernel=k.index)
+        try:
+            plan.setShifts(shifts)
+            if mode != DD_STEP_TWO and zapped is not None:
+                plan.setZappedChannels(zapped)
+            if mode != DD_STEP_ONE:
+                plan.setBeamMapping(mapping if mapping is not None
+                                    else np.zeros(obs.getNrSynthesizedBeams() *
+                                                  lay.mapping_row_elems, np.uint32))
+            mean, std = _time_plan(plan, d_in, d_out, warmup, iterations)
+        except DedispersionError as e:
+            # a configuration this problem cannot run (e.g. its window does
+            # not fit in shared memory) is skipped, as the reference's tuner
+            # skips configurations that fail (src/DedispersionTuning.cpp:396-409)
+            if e.status in (DD_ERR_UNSUPPORTED, DD_ERR_INVALID_ARGUMENT):
+                continue
+            raise
+        finally:
+            plan.close()
+        out.append(TuneResult(k.index, k.name, k.conf, mean, std, 1e-9 * units / (mean * 1e-3),
+                              time.perf_counter() - t0))
+    out.sort(key=lambda r: r.mean_ms)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# learned tuning
+
+BITS = (2, 4, 8, 32)
+VARIANTS = ("PermuteMad", "Permute", "PermuteHalf", "MaskHigh")
+# Delay per unit DM of the lowest channel, in samples, for the study band
+# (1220-1520 MHz at 81.92 us); the window spread of a tile scales with it.
+STUDY_SHIFT0 = 12.1
+
+
+@dataclass
+class Shape:
+    """One tuning problem: geometry, input width and subbands (0: single step)."""
+
+    channels: int
+    dms: int
+    samples: int
+    bits: int
+    subbands: int
+    dm_step: float = 0.2
+    seed: int = 0
+
+    def mode(self) -> int:
+        return DD_STEP_ONE if self.subbands else DD_SINGLE_STEP
+
+
+def study_shapes(count: int = 400, seed: int = 4242) -> list[Shape]:
+    """Seeded shapes over channels 256-4096, DMs 256-8192, samples 4096-65536,
+    input bits 2/4/8/32, subbands 0/16/32/64/128."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        sb = int(rng.choice([0, 16, 32, 64, 128]))
+        ch = int(2 ** rng.uniform(8, 12))
+        if sb:
+            ch = max(sb * 2, ch // sb * sb)
+        out.append(Shape(channels=ch, dms=int(2 ** rng.uniform(8, 13)) // 32 * 32 or 32,
+                         samples=int(2 ** rng.uniform(12, 16)) // 1024 * 1024,
+                         bits=int(rng.choice(BITS)), subbands=sb,
+                         dm_step=float(np.float32(rng.uniform(0.05, 0.5))), seed=seed + i))
+    return out
+
+
+def measured_observation(s: Shape, padding: int, max_dms: int = 256, max_samples: int = 8192):
+    """The shape's observation cut to at most max_dms DM trials (per step) and
+    max_samples samples, keeping channels, DM step and input width: the
+    per-DM-sample cost of a tile depends on those, not on the trial count."""
+    S = min(s.samples, max_samples)
+    bw = 300.0 / s.channels
+    if s.subbands:
+        d1 = max(1, min(s.dms // 32, max_dms // 4))
+        return syn.make_observation(s.channels, 1220.0, bw, 81.92e-6, S, 32, 0.0, s.dm_step,
+                                    subbands=s.subbands, dms1=d1, first_dm1=0.0,
+                                    dm_step1=s.dm_step * 32, padding=padding)
+    return syn.make_observation(s.channels, 1220.0, bw, 81.92e-6, S, min(s.dms, max_dms), 0.0,
+                                s.dm_step, padding=padding)
+
+
+def features(s: Shape, conf: DedispersionConf, name: str) -> np.ndarray:
+    """Shape and configuration features of one (problem, configuration) pair."""
+    shift0 = STUDY_SHIFT0
+    tile_d = conf.nrThreadsD1 * conf.nrItemsD1
+    spread = shift0 * s.dm_step * (32 if s.subbands else 1) * tile_d
+    rows = s.channels // s.subbands if s.subbands else s.channels
+    f = [math.log2(s.channels), math.log2(rows), math.log2(max(1, s.dms)),
+         math.log2(max(1, s.samples)), math.log2(s.subbands + 1), math.log2(1 + spread),
+         math.log2(conf.nrItemsD0), math.log2(conf.nrItemsD1), math.log2(conf.nrThreadsD1),
+         math.log2(conf.unroll), math.log2(tile_d), math.log2(32 * conf.nrItemsD0),
+         float(s.subbands > 0)]
+    f += [float(s.bits == b) for b in BITS]
+    f += [float(name.endswith("_v" + str(i))) for i in range(len(VARIANTS))]
+    return np.array(f, np.float32)
+
+
+@dataclass
+class StudyRecord:
+    shape: Shape
+    results: list  # TuneResult, all configurations of the family
+    units: float   # DM-samples of the measured problem
+
+
+def collect(shapes: list[Shape], padding: int = 128, iterations: int = 3, device: int = 0,
+            log=None) -> list[StudyRecord]:
+    """Time every configuration of every shape (the exhaustive sweep)."""
+    import torch
+    records = []
+    for i, s in enumerate(shapes):
+        obs = measured_observation(s, padding)
+        mode = s.mode()
+        shifts = getShifts(obs, padding)
+        zapped = syn.zapped_mask(s.channels, 0.05, s.seed, padding)
+        lay = layout(obs, mode, s.bits, padding)
+        g = torch.Generator(device=f"cuda:{device}")
+        g.manual_seed(s.seed)
+        if s.bits == 32:
+            d_in = torch.rand(lay.input_bytes // 4, generator=g, device=f"cuda:{device}")
+        elif s.bits == 16:
+            d_in = torch.randint(0, 60000, (lay.input_bytes // 2,), generator=g,
+                                 device=f"cuda:{device}", dtype=torch.int32).to(torch.int16)
+        else:
+            d_in = torch.randint(0, 255, (lay.input_bytes,), generator=g, device=f"cuda:{device}",
+                                 dtype=torch.uint8)
+        d_out = torch.empty(lay.output_bytes // 4, dtype=torch.float32, device=f"cuda:{device}")
+        res = sweep(obs, mode, s.bits, padding, shifts, zapped, None, d_in, d_out,
+                    iterations=iterations, device=device)
+        units = (obs.getNrDMs(True) * obs.getNrSubbands() * obs.getNrSamplesPerBatch(True)
+                 if s.subbands else obs.getNrDMs() * obs.getNrSamplesPerBatch())
+        records.append(StudyRecord(s, res, units))
+        if log and (i % 20 == 0):
+            log(f"shape {i}/{len(shapes)}: {s} best {res[0].name} {res[0].mean_ms:.3f} ms")
+    return records
+
+
+def dataset(records: list[StudyRecord]):
+    X, y, owner = [], [], []
+    for r_i, rec in enumerate(records):
+        for res in rec.results:
+            X.append(features(rec.shape, res.conf, res.name))
+            y.append(math.log(res.mean_ms * 1e-3 / rec.units))
+            owner.append(r_i)
+    return np.stack(X), np.array(y, np.float32), np.array(owner)
+
+
+class LearnedTuner:
+    """MLP over (shape, configuration) features, trained on measured timings."""
+
+    def __init__(self, hidden: int = 128, layers: int = 3, seed: int = 0, device: int = 0):
+        self.hidden, self.layers, self.seed, self.device = hidden, layers, seed, device
+        self.model = None
+        self.mu = self.sd = None
+        self.train_loss = None
+
+    def fit(self, X: np.ndarray, y: np.ndarray, steps: int = 3000, lr: float = 1e-3) -> float:
+        from .costmodel import MLP
+        self.mu, self.sd = X.mean(axis=0), X.std(axis=0) + 1e-6
+        self.ymu, self.ysd = float(y.mean()), float(y.std() + 1e-6)
+        self.model = MLP(X.shape[1], self.hidden, self.layers, self.seed, self.device)
+        self.train_loss = self.model.train((X - self.mu) / self.sd, (y - self.ymu) / self.ysd,
+                                           steps, lr)
+        return self.train_loss
+
+    def predict(self, X: np.ndarray) -> np.ndarray:
+        return self.model.forward((X - self.mu) / self.sd) * self.ysd + self.ymu
+
+    def rank(self, shape: Shape, candidates) -> list:
+        X = np.stack([features(shape, k.conf, k.name) for k in candidates])
+        order = np.argsort(self.predict(X))
+        return [candidates[i] for i in order]
+
+
+def evaluate(records, tuner: LearnedTuner, test_idx, k: int = 4, seed: int = 7) -> dict:
+    """Top-k by model, k random and the default configuration against the
+    exhaustive best on held-out shapes; tuning wall time with and without."""
+    rng = np.random.default_rng(seed)
+    model_r, random_r, default_r, within5 = [], [], [], 0
+    t_exhaustive = t_learned = 0.0
+    for i in test_idx:
+        rec = records[i]
+        by_index = {r.kernel: r for r in rec.results}
+        best = rec.results[0].mean_ms
+        cands = [kk for kk in kernels() if kk.index in by_index]
+        t0 = time.perf_counter()
+        ranked = tuner.rank(rec.shape, cands)[:k]
+        infer = time.perf_counter() - t0
+        chosen = min(by_index[c.index].mean_ms for c in ranked)
+        model_r.append(best / chosen)
+        within5 += best / chosen >= 0.95
+        rnd = rng.choice(len(cands), size=min(k, len(cands)), replace=False)
+        random_r.append(best / min(by_index[cands[j].index].mean_ms for j in rnd))
+        default_r.append(best / by_index[cands[0].index].mean_ms)
+        t_exhaustive += sum(r.wall_s for r in rec.results)
+        t_learned += infer + sum(by_index[c.index].wall_s for c in ranked)
+    return {"held_out_shapes": len(test_idx), "k": k,
+            "top_k_vs_best_mean": float(np.mean(model_r)),
+            "top_k_vs_best_median": float(np.median(model_r)),
+            "top_k_vs_best_worst": float(np.min(model_r)),
+            "shapes_within_5pct": int(within5),
+            "random_k_vs_best_mean": float(np.mean(random_r)),
+            "default_vs_best_mean": float(np.mean(default_r)),
+            "tuning_time_exhaustive_s": t_exhaustive, "tuning_time_learned_s": t_learned,
+            "tuning_time_ratio": t_learned / t_exhaustive if t_exhaustive else None}
+
+
+def study(count: int = 400, train_fraction: float = 0.8, steps: int = 3000, k: int = 4,
+          device: int = 0, log=print) -> dict:
+    """The full learned-tuning study: sweep, train on 80 %, evaluate on 20 %."""
+    shapes = study_shapes(count)
+    t0 = time.perf_counter()
+    records = collect(shapes, device=device, log=log)
+    t_collect = time.perf_counter() - t0
+    rng = np.random.default_rng(1)
+    perm = rng.permutation(len(records))
+    n_train = int(round(train_fraction * len(records)))
+    train_idx, test_idx = perm[:n_train], perm[n_train:]
+    X, y, owner = dataset(records)
+    mask = np.isin(owner, train_idx)
+    tuner = LearnedTuner(device=device)
+    t0 = time.perf_counter()
+    loss = tuner.fit(X[mask], y[mask], steps=steps)
+    t_train = time.perf_counter() - t0
+    test_mask = np.isin(owner, test_idx)
+    pred = tuner.predict(X[test_mask])
+    rep = evaluate(records, tuner, test_idx, k=k)
+    rep["by_k"] = {str(kk): {key: v for key, v in evaluate(records, tuner, test_idx, k=kk).items()
+                             if key in ("top_k_vs_best_mean", "shapes_within_5pct",
+                                        "tuning_time_ratio")} for kk in (1, 2, 3, 4, 6)}
+    rep.update({"shapes": count, "configurations_per_shape": float(np.mean(
+        [len(r.results) for r in records])), "train_rows": int(mask.sum()),
+        "train_loss_normalised": loss,
+        "held_out_rmse_log_time": float(np.sqrt(np.mean((pred - y[test_mask]) ** 2))),
+        "collect_s": t_collect, "train_s": t_train,
+        "network": "3 x 128 ReLU, bf16 weights, fp32 accumulation, trained by the library's "
+                   "CUDA kernels (Adam, full batch)"})
+    return rep
+
+
+# ---------------------------------------------------------------------------
+# command line: the reference's DedispersionTuning switches
+
+def _args(argv):
+    ap = argparse.ArgumentParser(prog="python -m dedispersion_gb300.tuning",
+                                 prefix_chars="-", allow_abbrev=False)
+    for flag in ("-single_step", "-step_one", "-step_two", "-best"):
+        ap.add_argument(flag, action="store_true")
+    for flag, typ in (("-iterations", int), ("-padding", int), ("-beams", int),
+                      ("-synthesized_beams", int), ("-samples", int), ("-sampling_time", float),
+                      ("-min_freq", float), ("-channel_bandwidth", float), ("-channels", int),
+                      ("-subbands", int), ("-dms", int), ("-dm_first", float), ("-dm_step", float),
+                      ("-subbanding_dms", int), ("-subbanding_dm_first", float),
+                      ("-subbanding_dm_step", float), ("-input_bits", int),
+                      ("-min_threads", int), ("-max_threads", int), ("-max_items", int),
+                      ("-max_unroll", int)):
+        ap.add_argument(flag, type=typ)
+    ap.add_argument("-zapped_channels")
+    ap.add_argument("-device_name", default="GB300")
+    ap.add_argument("-tuned_file")
+    return ap.parse_args(argv)
+
+
+def main(argv=None) -> int:
+    a = _args(argv if argv is not None else sys.argv[1:])
+    if a.single_step + a.step_one + a.step_two != 1:
+        print("Mutually exclusive modes, select one: -single_step -step_one -step_two",
+              file=sys.stderr)
+        return 1
+    from . import Observation
+    o = Observation()
+    o.setNrBeams(a.beams or 1)
+    o.setNrSamplesPerBatch(a.samples)
+    o.setSamplingTime(a.sampling_time)
+    bits = a.input_bits or 8
+    if a.single_step:
+        o.setNrSynthesizedBeams(a.synthesized_beams or 1)
+        o.setFrequencyRange(1, a.channels, a.min_freq, a.channel_bandwidth)
+        o.setDMRange(a.dms, a.dm_first, a.dm_step)
+        mode = DD_SINGLE_STEP
+    else:
+        o.setNrSynthesizedBeams(a.synthesized_beams or 1)
+        o.setFrequencyRange(a.subbands, a.channels, a.min_freq, a.channel_bandwidth)
+        o.setDMRange(a.subbanding_dms, a.subbanding_dm_first or 0.0, a.subbanding_dm_step or 0.0,
+                     True)
+        o.setDMRange(a.dms, a.dm_first, a.dm_step)
+        mode = DD_STEP_ONE if a.step_one else DD_STEP_TWO
+    padding = a.padding
+    shifts = getShifts(o, padding)
+    from . import getShiftsStepTwo
+    shifts2 = getShiftsStepTwo(o, padding) if not a.single_step else None
+    zapped = np.zeros(o.getNrChannels(padding // 4), np.uint32)
+    if a.zapped_channels:
+        for tok in open(a.zapped_channels).read().split():
+            c = int(tok)
+            if 0 <= c < o.getNrChannels():
+                zapped[c] = 1
+    # dispersed lengths as DedispersionTuning sets them (src/DedispersionTuning.cpp:131-143)
+    if a.single_step:
+        o.setNrSamplesPerDispersedBatch(syn.dispersed_samples(a.samples, shifts[0], a.dm_first,
+                                                              a.dms, a.dm_step))
+    else:
+        s1 = syn.dispersed_samples(a.samples, shifts2[0], a.dm_first, a.dms, a.dm_step)
+        o.setNrSamplesPerBatch(s1, True)
+        o.setNrSamplesPerDispersedBatch(syn.dispersed_samples(
+            s1, shifts[0], a.subbanding_dm_first or 0.0, a.subbanding_dms,
+            a.subbanding_dm_step or 0.0), True)
+    cands = []
+    for k in family_kernels(mode, bits):
+        c = k.conf
+        threads = c.nrThreadsD0 * c.nrThreadsD1
+        items = c.nrItemsD0 * c.nrItemsD1
+        if a.min_threads and threads < a.min_threads:
+            continue
+        if a.max_threads and threads > a.max_threads:
+            continue
+        if a.max_items and items > a.max_items:
+            continue
+        if a.max_unroll and c.unroll > a.max_unroll:
+            continue
+        cands.append(k)
+    res = sweep(o, mode, bits, padding, shifts2 if a.step_two else shifts,
+                zapped if not a.step_two else None, None, iterations=a.iterations or 3,
+                candidates=cands)
+    if a.best:
+        best = res[0]
+        line = f"{a.dms if not a.step_one else a.subbanding_dms} {best.conf.print()}"
+        print(line)
+        if a.tuned_file:
+            from . import writeTunedDedispersionConf
+            writeTunedDedispersionConf(a.tuned_file, a.device_name,
+                                       a.dms if not a.step_one else a.subbanding_dms, best.conf)
+        return 0
+    print("# nrBeams nrSynthesizedBeams nrSubbandingDMs nrDMs nrSubbands nrChannels "
+          "nrZappedChannels nrSamplesSubbanding nrSamples *configuration* GFLOP/s time "
+          "stdDeviation COV\n")
+    nz = int(zapped[:o.getNrChannels()].sum())
+    for r in res:
+        cov = r.std_ms / r.mean_ms if r.mean_ms else 0.0
+        print(f"{o.getNrBeams()} {o.getNrSynthesizedBeams()} {o.getNrDMs(True)} {o.getNrDMs()} "
+              f"{o.getNrSubbands()} {o.getNrChannels()} {nz} {o.getNrSamplesPerBatch(True)} "
+              f"{o.getNrSamplesPerBatch()} {r.conf.print()} {r.gflops:.3f} "
+              f"{r.mean_ms * 1e-3:.6f} {r.std_ms * 1e-3:.6f} {cov:.6f}")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

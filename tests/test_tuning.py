@@ -1,0 +1,68 @@
+"""The exhaustive tuner (DedispersionTuning's role) and the learned tuner."""
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import dedispersion_gb300 as dd
+from dedispersion_gb300 import tuning
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def test_study_shapes_are_seeded_and_in_range(engine):
+    a, b = tuning.study_shapes(50), tuning.study_shapes(50)
+    assert a == b
+    for s in a:
+        assert 256 <= s.channels <= 4096 and s.bits in (2, 4, 8, 32)
+        assert 4096 <= s.samples <= 65536 and 32 <= s.dms <= 8192
+        assert s.subbands in (0, 16, 32, 64, 128)
+        if s.subbands:
+            assert s.channels % s.subbands == 0
+
+
+def test_features_distinguish_configurations(engine):
+    s = tuning.study_shapes(1)[0]
+    ks = tuning.family_kernels(s.mode(), s.bits)
+    F = np.stack([tuning.features(s, k.conf, k.name) for k in ks])
+    assert np.isfinite(F).all()
+    assert len({tuple(r) for r in F}) == len(ks)
+
+
+@pytest.mark.gpu
+def test_exhaustive_cli_best_line(gpu, tmp_path):
+    tuned = tmp_path / "tuned.conf"
+    args = [sys.executable, "-m", "dedispersion_gb300.tuning", "-iterations", "2", "-single_step",
+            "-padding", "128", "-beams", "1", "-synthesized_beams", "1", "-samples", "4096",
+            "-sampling_time", "0.00008192", "-min_freq", "1220", "-channel_bandwidth", "0.5",
+            "-channels", "256", "-dms", "128", "-dm_first", "0", "-dm_step", "0.2", "-best",
+            "-tuned_file", str(tuned), "-device_name", "GB300"]
+    p = subprocess.run(args, cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert p.returncode == 0, p.stderr
+    fields = p.stdout.split()
+    assert fields[0] == "128" and len(fields) == 10
+    conf = dd.readTunedDedispersionConf(str(tuned), "GB300", 128)
+    assert conf.print() == " ".join(fields[1:])
+
+
+@pytest.mark.gpu
+def test_learned_tuner_beats_random_choice(gpu):
+    shapes = tuning.study_shapes(48, seed=99)
+    # small problems keep the sweep short
+    old = tuning.measured_observation
+    tuning.measured_observation = lambda s, p: old(s, p, max_dms=64, max_samples=2048)
+    try:
+        records = tuning.collect(shapes, iterations=2)
+    finally:
+        tuning.measured_observation = old
+    X, y, owner = tuning.dataset(records)
+    train = np.arange(36)
+    test = np.arange(36, 48)
+    t = tuning.LearnedTuner(seed=3)
+    t.fit(X[np.isin(owner, train)], y[np.isin(owner, train)], steps=1500)
+    rep = tuning.evaluate(records, t, test, k=4)
+    assert rep["top_k_vs_best_mean"] >= rep["random_k_vs_best_mean"]
+    assert rep["top_k_vs_best_mean"] > 0.8
+    assert rep["tuning_time_ratio"] < 0.5
