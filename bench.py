@@ -77,6 +77,27 @@ def dist_env():
     return rank, world, local
 
 
+def beam_seed(rank):
+    """Each rank dedisperses its own beam (weak scaling): beams are independent,
+    so ranks share no data and no collective sits on the data path."""
+    return 1 + rank
+
+
+def max_over_ranks(seconds, pg, device):
+    """The job's elapsed time: the slowest rank's (all_reduce MAX)."""
+    if pg is None:
+        return seconds
+    import torch
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(world, steps, dms, samples, seconds):
+    """Whole-job DM-samples/s: every rank's units over the slowest rank's time."""
+    return world * steps * dms * samples / seconds
+
+
 def workload(seed=1):
     import dedispersion_gb300 as dd
     from dedispersion_gb300 import synthetic as syn
@@ -332,7 +353,7 @@ def main():
         tdist.init_process_group("nccl", device_id=torch.device("cuda", local))
         pg = tdist
 
-    obs, shifts, zapped, mapping, inp = workload(seed=1 + rank)
+    obs, shifts, zapped, mapping, inp = workload(seed=beam_seed(rank))
     S, D = obs.getNrSamplesPerBatch(), obs.getNrDMs()
     live = int((zapped[:1536] == 0).sum())
     lay = dd.layout(obs, dd.DD_SINGLE_STEP, 8, PADDING, shifts)
@@ -366,13 +387,8 @@ def main():
         ms = e0.elapsed_time(e1)
     plan.check(stream)
     clocks = clk.summary()
-    t_dev = ms / 1e3
-    if pg is not None:
-        t = torch.tensor([t_dev], device=f"cuda:{local}")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        t_dev = float(t.item())
-    units = world * args.steps * D * S
-    value = units / t_dev
+    t_dev = max_over_ranks(ms / 1e3, pg, f"cuda:{local}")
+    value = job_value(world, args.steps, D, S, t_dev)
     per_launch_s = t_dev / args.steps
     if args.kernel_only:
         if rank == 0:
@@ -395,12 +411,8 @@ def main():
     for _ in range(e2e_steps):
         dd.dedispersion(obs, zapped, mapping, in_np, out_np, shifts, PADDING, 8)
     barrier()
-    t_e2e = time.perf_counter() - t
-    if pg is not None:
-        tt = torch.tensor([t_e2e], device=f"cuda:{local}")
-        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
-        t_e2e = float(tt.item())
-    e2e_value = world * e2e_steps * D * S / t_e2e
+    t_e2e = max_over_ranks(time.perf_counter() - t, pg, f"cuda:{local}")
+    e2e_value = job_value(world, e2e_steps, D, S, t_e2e)
 
     batched = bench_batched(torch, local) if not args.no_batched else None
     served = bench_served(local) if not args.no_served else None
