@@ -472,6 +472,12 @@ class Plan:
         check(lib().dd_plan_get_conf(self._h, C.byref(c)))
         return DedispersionConf.from_c(c)
 
+    def adds(self) -> int:
+        """Integer adds one run performs (tile padding included)."""
+        n = C.c_uint64(0)
+        check(lib().dd_plan_adds(self._h, C.byref(n)))
+        return n.value
+
     def close(self) -> None:
         if self._h:
             lib().dd_plan_destroy(self._h)

@@ -123,6 +123,7 @@ SIGNATURES = {
     "dd_plan_check": (C.c_int, [_P, _P]),
     "dd_plan_launches": (C.c_int, [_P, _U32P]),
     "dd_plan_get_conf": (C.c_int, [_P, _CONF]),
+    "dd_plan_adds": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "dd_plan_destroy": (C.c_int, [_P]),
     "dd_batch_create": (C.c_int, [C.POINTER(_P), C.c_int]),
     "dd_batch_add": (C.c_int, [_P, _OBS, C.c_uint32, C.c_uint32, _F32P, _U32P, _U32P, _P, _P,

@@ -20,6 +20,7 @@
 
 #include "../../include/dedisp_gb300.h"
 #include "dd_internal.h"
+#include "dd_shared_plan.h"
 
 namespace {
 
@@ -179,6 +180,10 @@ const dd::KernelInfo *find_kernel(dd_mode mode, uint32_t bits, const dd_conf &c)
     if (c.threads_d0 != 32u || c.threads_d1 != (uint32_t)k.warps_d) continue;
     if (c.items_d0 != (uint32_t)k.items_t || c.items_d1 != (uint32_t)k.items_d) continue;
     if (c.unroll != (uint32_t)k.channels) continue;
+    // items_d2 = rows per shared partial sum marks the shared family.
+    const bool shared = c.items_d2 == (uint32_t)dd::kSharedRows;
+    if (shared != (k.family == dd::kFamilyShared8)) continue;
+    if (shared && mode != DD_SINGLE_STEP) continue;
     return &k;
   }
   return nullptr;
@@ -188,7 +193,8 @@ dd_conf conf_of(const dd::KernelInfo &k) {
   dd_conf c{};
   c.split_batches = 0; c.local_mem = 1; c.unroll = k.channels;
   c.threads_d0 = 32; c.threads_d1 = k.warps_d; c.threads_d2 = 1;
-  c.items_d0 = k.items_t; c.items_d1 = k.items_d; c.items_d2 = 1;
+  c.items_d0 = k.items_t; c.items_d1 = k.items_d;
+  c.items_d2 = k.family == dd::kFamilyShared8 ? dd::kSharedRows : 1;
   return c;
 }
 
@@ -243,6 +249,12 @@ struct dd_plan {
   uint16_t *d_delay_rel = nullptr;
   size_t cap_delay_rel = 0;
   bool use_delay_tables = false;
+  // Shared-partial-sum tables (kFamilyShared8 only).
+  dd::SharedTables shared;
+  dd::SharedStage *d_stages = nullptr;
+  uint32_t *d_tile_stage = nullptr;
+  uint16_t *d_pool = nullptr;
+  size_t cap_stages = 0, cap_tile_stage = 0, cap_pool = 0;
   std::string invalid;  // why the tables are not usable (empty when ready)
   bool ready = false;
 };
@@ -355,11 +367,31 @@ dd_status rebuild(dd_plan *p) {
     return fail(DD_ERR_INVALID_ARGUMENT,
                 "rows hold %u samples but %u output samples + max delay %u are needed",
                 d.row_samples, d.nr_samples, max_delay);
+  int dev_max = 0, sm_max = 0;
+  {
+    DeviceGuard g(p->device);
+    DD_CUDA(cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device),
+            "query shared memory");
+    DD_CUDA(cudaDeviceGetAttribute(&sm_max, cudaDevAttrMaxSharedMemoryPerMultiprocessor,
+                                   p->device), "query shared memory");
+  }
+  const bool shared = k.family == dd::kFamilyShared8;
+  if (shared) {
+    if (p->mode != DD_SINGLE_STEP || p->bits > 8)
+      return fail(DD_ERR_UNSUPPORTED, "kernel %s computes single-step 1/2/4/8-bit input only",
+                  k.name);
+    // One CTA per SM: the whole opt-in shared memory of a block.
+    const size_t budget = (size_t)dev_max;
+    (void)sm_max;
+    const std::string why = dd::build_shared_tables(k, p->delay_shift, d.first_dm, d.dm_step,
+                                                    d.nr_dms, p->bits, budget, &p->shared);
+    if (!why.empty()) return fail(DD_ERR_UNSUPPORTED, "tile %s: %s", k.name, why.c_str());
+  }
   // Delay table: the offsets of each DM tile's delays from the delay of its
   // first DM, per delay row (the same float order as the device's
   // dev_delay).  16-bit offsets: skipped if a spread does not fit.
   const size_t rows = p->delay_shift.size();
-  p->use_delay_tables = spread < 65536 && rows > 0 && p->tiles_d > 0;
+  p->use_delay_tables = !shared && spread < 65536 && rows > 0 && p->tiles_d > 0;
   if (p->use_delay_tables) {
     p->delay_rel.assign((size_t)p->tiles_d * rows * k.tile_d, 0);
     // DM values in the reference's order (firstDM + dm * dmStep, each op
@@ -384,14 +416,8 @@ dd_status rebuild(dd_plan *p) {
   }
   const uint32_t bits = family_bits(p->mode, p->bits) == 8 ? p->bits : family_bits(p->mode, p->bits);
   const uint32_t a = dd::window_alignment_samples(bits);
-  p->win = ((k.tile_t + spread + a + 8) + 15) / 16 * 16;
-  p->smem = dd::kernel_smem_bytes(k, p->win, bits);
-  int dev_max = 0;
-  {
-    DeviceGuard g(p->device);
-    DD_CUDA(cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device),
-            "query shared memory");
-  }
+  p->win = shared ? 0 : ((k.tile_t + spread + a + 8) + 15) / 16 * 16;
+  p->smem = shared ? p->shared.smem : dd::kernel_smem_bytes(k, p->win, bits);
   if (p->smem > (size_t)dev_max)
     return fail(DD_ERR_UNSUPPORTED,
                 "tile %s needs %zu bytes of shared memory (window %u samples), device allows %d; "
@@ -422,6 +448,9 @@ dd_status rebuild(dd_plan *p) {
   if (p->use_delay_tables) {
     if (p->delay_rel.size() > p->cap_delay_rel) {
       if (p->d_delay_rel) cudaFree(p->d_delay_rel);
+    if (p->d_stages) cudaFree(p->d_stages);
+    if (p->d_tile_stage) cudaFree(p->d_tile_stage);
+    if (p->d_pool) cudaFree(p->d_pool);
       p->d_delay_rel = nullptr;
       DD_CUDA(cudaMalloc(&p->d_delay_rel, p->delay_rel.size() * sizeof(uint16_t)),
               "allocate delay table");
@@ -430,6 +459,26 @@ dd_status rebuild(dd_plan *p) {
     DD_CUDA(cudaMemcpy(p->d_delay_rel, p->delay_rel.data(),
                        p->delay_rel.size() * sizeof(uint16_t), cudaMemcpyHostToDevice),
             "upload delay table");
+  }
+  if (shared) {
+    auto upload = [&](auto **dptr, size_t *cap, const auto &v, const char *what) -> dd_status {
+      using T = typename std::decay<decltype(v)>::type::value_type;
+      const size_t n = std::max<size_t>(1, v.size());
+      if (n > *cap || !*dptr) {
+        if (*dptr) cudaFree(*dptr);
+        *dptr = nullptr;
+        DD_CUDA(cudaMalloc(reinterpret_cast<void **>(dptr), n * sizeof(T)), what);
+        *cap = n;
+      }
+      if (!v.empty())
+        DD_CUDA(cudaMemcpy(*dptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), what);
+      return DD_OK;
+    };
+    dd_status us = upload(&p->d_stages, &p->cap_stages, p->shared.stages, "upload stage table");
+    if (!us) us = upload(&p->d_tile_stage, &p->cap_tile_stage, p->shared.tile_stage,
+                         "upload tile stage table");
+    if (!us) us = upload(&p->d_pool, &p->cap_pool, p->shared.pool, "upload stage pool");
+    if (us) return us;
   }
   // The attribute is a cap shared by every plan of this kernel: set it to the
   // device maximum so that no plan lowers it below another plan's need.
@@ -481,6 +530,15 @@ dd_status plan_problem(const dd_plan *p, const void *d_input, float *d_output,
   if (p->use_delay_tables) {
     P.delay_rows = (uint32_t)p->delay_shift.size();
     P.delay_rel = p->d_delay_rel;
+  }
+  if (p->kinfo->family == kFamilyShared8) {
+    P.stages = p->d_stages;
+    P.tile_stage = p->d_tile_stage;
+    P.pool = p->d_pool;
+    P.cw = p->shared.cw;
+    P.psw = p->shared.psw;
+    P.slots = p->shared.slots;
+    P.table_bytes = p->shared.table_bytes;
   }
   *out = P;
   if (rows_per_group)
@@ -849,6 +907,21 @@ dd_status dd_plan_get_conf(const dd_plan *p, dd_conf *conf) {
   return DD_OK;
 }
 
+dd_status dd_plan_adds(const dd_plan *p, uint64_t *adds) {
+  if (!p || !adds) return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (!p->ready)
+    return fail(DD_ERR_INVALID_ARGUMENT, p->have_shifts ? "plan tables are invalid: %s"
+                                                        : "plan has no shift table%s",
+                p->have_shifts ? p->invalid.c_str() : "");
+  const dd::KernelInfo &k = *p->kinfo;
+  const uint64_t per_tile = k.family == dd::kFamilyShared8
+                                ? p->shared.adds_partial + p->shared.adds_series
+                                : (p->nr_groups ? p->entries.size() / p->nr_groups : 0) *
+                                      (uint64_t)k.tile_d * k.tile_t * p->tiles_d;
+  *adds = per_tile * p->nr_groups * p->tiles_t;
+  return DD_OK;
+}
+
 dd_status dd_plan_destroy(dd_plan *p) {
   if (!p) return DD_OK;
   {
@@ -857,6 +930,9 @@ dd_status dd_plan_destroy(dd_plan *p) {
     if (p->d_entries) cudaFree(p->d_entries);
     if (p->d_status) cudaFree(p->d_status);
     if (p->d_delay_rel) cudaFree(p->d_delay_rel);
+    if (p->d_stages) cudaFree(p->d_stages);
+    if (p->d_tile_stage) cudaFree(p->d_tile_stage);
+    if (p->d_pool) cudaFree(p->d_pool);
   }
   delete p;
   return DD_OK;

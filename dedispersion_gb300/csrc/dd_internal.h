@@ -37,6 +37,29 @@ struct EntryDesc {
   uint32_t delay_row;   // row of the precomputed delay tables (when present)
 };
 
+// One pipeline stage of the shared-partial-sum family (kFamilyShared8), for
+// one DM tile: up to 4 subgroups of up to kSharedRows consecutive rows of a
+// group (32 rows).  For every DM d of the tile a subgroup's delays are
+// base(d) + rel(row, d), base(d) = the least delay of its rows.  DMs whose
+// relative-delay vectors are equal share one partial-sum series
+//   P_v[u] = sum_rows in_row[t0 + bmin + u + rel_v(row)],
+// and DM d adds P_{v(d)}[t + base(d) - bmin]: the same integer sum as the
+// direct form with fewer adds.  The stage table (in `pool`, laid out as
+// dd_shared.cuh describes) holds the subgroups' series programs and each
+// DM's series offsets.
+struct SharedStage {
+  uint32_t pool;         // u16 index of the stage table in the pool (x8)
+  uint32_t row_first;    // first row of the stage within its group
+  uint16_t nrows;        // rows in the stage (<= 32)
+  uint16_t nsub;         // subgroups (<= 4)
+  uint16_t table_bytes;  // bytes of the stage table (multiple of 16)
+  uint16_t nitems;       // phase-A work items
+  uint32_t bmin[4];      // window start of each subgroup relative to t0 (x4)
+  uint8_t row_sub[32];   // subgroup of each row
+};
+static_assert(sizeof(SharedStage) == 64, "stage descriptor layout");
+constexpr int kSharedRows = 8;
+
 // Device status word bits, set with atomicOr by a kernel.
 enum : uint32_t {
   kStatusTimeout = 1u,  // a bounded wait on a bulk copy ran out
@@ -69,12 +92,20 @@ struct ProblemDesc {
   //   delay_rel[(t * delay_rows + r) * tile_d + j]
   //       = delay(r, min(d0 + j, nr_dms - 1)) - delay(r, d0)
   const uint16_t *delay_rel;
+  // Shared-partial-sum family only (NULL otherwise).
+  const SharedStage *stages;    // all DM tiles' stages
+  const uint32_t *tile_stage;   // [tiles_d + 1]: first stage of each DM tile
+  const uint16_t *pool;         // stage tables
+  uint32_t cw;                  // words per shifted copy of a staged row (even)
+  uint32_t psw;                 // words per copy of one partial-sum series
+  uint32_t slots;               // partial-sum series slots per stage
+  uint32_t table_bytes;         // largest stage table (multiple of 16)
 };
 
 // One entry of the kernel registry: a compiled tile configuration.
 struct KernelInfo {
   const char *name;
-  int family;       // kFamilySwar8 or kFamilyScalar
+  int family;       // kFamilySwar8, kFamilyScalar or kFamilyShared8
   int elem_bits;    // swar8: 8 (covers 1/2/4/8); scalar: 16 or 32
   int items_t;      // samples per thread
   int items_d;      // DMs per thread
@@ -89,7 +120,7 @@ struct KernelInfo {
                  cudaStream_t stream);
 };
 
-enum { kFamilySwar8 = 0, kFamilyScalar = 1 };
+enum { kFamilySwar8 = 0, kFamilyScalar = 1, kFamilyShared8 = 2 };
 
 // Registry of compiled configurations (dd_kernels.cu).
 const KernelInfo *kernel_registry(int *count);

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include "dd_device.cuh"
+#include "dd_shared.cuh"
 
 namespace dd {
 
@@ -32,6 +33,25 @@ __global__ void __launch_bounds__(32 * TY, (TY >= 8 ? 2 : 4))
   (void)scalar_tile<T, NS, NDT, TY, CH>(P, P.groups[g], dtile, ttile, smem, L, sc);
 }
 
+template <int NW, int ND, int TY>
+__global__ void __launch_bounds__(32 * TY, (TY >= 16 ? 1 : 2))
+    shared8_kernel(const ProblemDesc P) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  const SharedLayout L = make_shared_layout(P.cw, P.psw, P.slots, P.table_bytes, P.bits);
+  if (threadIdx.x == 0) {
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
+    for (int r = 0; r < kNRaw; ++r) mbar_init(bars + r, kSharedArrivals);
+    fence_mbar_init();
+  }
+  // The zero series that absent subgroups of a stage read.
+  uint32_t *zero = reinterpret_cast<uint32_t *>(smem + L.off_part) + L.zero_word;
+  for (uint32_t w = threadIdx.x; w < P.psw; w += blockDim.x) zero[w] = 0;
+  __syncthreads();
+  uint32_t g, dtile, ttile, sc = 0;
+  decode_tile(P, blockIdx.x, g, dtile, ttile);
+  (void)shared8_tile<NW, ND, TY>(P, P.groups[g], dtile, ttile, smem, L, sc);
+}
+
 template <int NW, int NDT, int TY, int CH, int VAR>
 void launch_swar8(const ProblemDesc &P, unsigned grid, size_t smem,
                   cudaStream_t stream) {
@@ -42,6 +62,12 @@ template <typename T, int NS, int NDT, int TY, int CH>
 void launch_scalar(const ProblemDesc &P, unsigned grid, size_t smem,
                    cudaStream_t stream) {
   scalar_kernel<T, NS, NDT, TY, CH><<<grid, 32 * TY, smem, stream>>>(P);
+}
+
+template <int NW, int ND, int TY>
+void launch_shared8(const ProblemDesc &P, unsigned grid, size_t smem,
+                    cudaStream_t stream) {
+  shared8_kernel<NW, ND, TY><<<grid, 32 * TY, smem, stream>>>(P);
 }
 
 #define DD_SWAR8(NW, NDT, TY, CH, VAR)                                        \
@@ -57,10 +83,19 @@ void launch_scalar(const ProblemDesc &P, unsigned grid, size_t smem,
    &launch_scalar<T, NS, NDT, TY, CH>}
 
 
+// Shared partial sums: items_t = samples per thread and DM (2 per word),
+// channels = rows per subgroup.
+#define DD_SHARED8(NW, ND, TY)                                                \
+  {"shared8_i" #NW "_d" #ND "_w" #TY, kFamilyShared8, 8, 2 * NW, ND, TY,      \
+   kSharedRows, 32 * TY, 64 * NW, TY * ND, 0,                                 \
+   reinterpret_cast<const void *>(&shared8_kernel<NW, ND, TY>),              \
+   &launch_shared8<NW, ND, TY>}
+
 // Parts of the registry, one per translation unit (compiled in parallel).
 const KernelInfo *kernels_swar8_a(int *count);
 const KernelInfo *kernels_swar8_b(int *count);
 const KernelInfo *kernels_swar8_c(int *count);
 const KernelInfo *kernels_scalar(int *count);
+const KernelInfo *kernels_shared8(int *count);
 
 }  // namespace dd

@@ -1,0 +1,343 @@
+// dd_shared.cuh -- the shared-partial-sum tile family (kFamilyShared8), for
+// input of 1, 2, 4 or 8 bits in single-step form.
+//
+// The direct form adds every live row into every DM of a tile.  Here the
+// rows of a group are cut into subgroups of up to kSharedRows consecutive
+// rows (chosen per DM tile on the host).  Within a subgroup, DM d's delays
+// are base(d) + rel(row, d); many DMs of a tile share the vector rel(., d)
+// (high-frequency rows barely move between DMs), so the tile computes each
+// distinct vector's partial sum once,
+//
+//   P_v[u] = sum_rows in_row[t0 + bmin + u + rel_v(row)]       (phase A)
+//
+// and every DM adds one series per subgroup at its own offset,
+//
+//   out[d][t] += P_{v(d)}[t + base(d) - bmin]                  (phase B).
+//
+// Phase A walks each subgroup's vectors in a chain chosen on the host so
+// that consecutive vectors differ in few rows: the first is summed over its
+// rows, each next one is the previous minus the rows that moved plus their
+// new samples.  Integer addition is exact and every intermediate value is a
+// sum of samples (non-negative), so the result equals the direct form's bit
+// for bit (8-bit rows: P <= 8 * 255, output < 2^24).  On the 1536-channel,
+// 2048-DM table the adds per DM-sample drop from 1459 to about 320.
+//
+// A pipeline stage holds up to kSubMax subgroups (kStageRows rows).  Per
+// stage: the rows arrive by bulk copies (one per row, plus the stage table)
+// in one of kNRaw slots; the CTA expands them into four byte-shifted copies
+// (any window read is one aligned 32-bit load); warps run the chains of
+// (subgroup, 31-group chunk) work items, writing each series in two copies
+// shifted by one sample (a read at any offset is aligned loads of two 16-bit
+// samples); then every thread adds kSubMax series into the 16-bit lanes of
+// its DMs (three-input adds; absent subgroups read a zero series), flushed
+// into 32-bit totals before a lane could pass 2^16.  Every wait is bounded
+// as in the direct families.
+#pragma once
+
+#include <cstdint>
+
+#include "dd_device.cuh"
+
+namespace dd {
+
+constexpr int kSubMax = 4;                              // subgroups per stage
+constexpr int kStageRows = kSubMax * kSharedRows;       // rows per stage
+constexpr uint32_t kSharedArrivals = 32;                // lanes of the issuing warp
+constexpr uint32_t kLaneSeries = 32;                    // series per 16-bit lane (32 * 2040 < 2^16)
+constexpr uint32_t kItemsMax = 32;                      // phase-A items per stage
+// Stage table (u16 units, in shared memory):
+//   [0] nsub [1] nrows [2] nitems [3..7] 0
+//   [8 + 4k] bmin_k lo, [+1] bmin_k hi, [+2] first row of k, [+3] program of k
+//   [kTabItems ..)         items: subgroup << 8 | chunk
+//   [kTabSeries ..)        per DM of the tile, kSubMax series offsets (words)
+//   programs, each 8-aligned: [n, nv, ng, dst0, 0 x4], 8 row offsets, then
+//   per next vector: u32 (h | dst << 16) and h x u32 (old | new << 16)
+constexpr uint32_t kTabItems = 8 + 4 * kSubMax;
+constexpr uint32_t kTabSeries = kTabItems + kItemsMax;
+
+struct SharedLayout {
+  uint32_t raw_bytes;  // bytes staged per row
+  uint32_t off_table, off_raw, off_copy, off_part, zero_word, total;
+};
+
+// Shared memory of one CTA: mbarriers, kNRaw stage tables, kNRaw x
+// kStageRows raw rows, the shifted copies of one stage's rows, `slots`
+// partial-sum series (two copies each) and one zero series.  Host and device
+// use this one formula.
+__host__ __device__ inline SharedLayout make_shared_layout(uint32_t cw, uint32_t psw,
+                                                           uint32_t slots,
+                                                           uint32_t table_bytes,
+                                                           uint32_t bits) {
+  SharedLayout L;
+  const uint32_t win = 4u * cw + 8u + align_samples(bits);  // samples per row
+  L.raw_bytes = round_up(win * bits / 8u, 16u);
+  L.off_table = 128;
+  L.off_raw = round_up(L.off_table + kNRaw * table_bytes, 128u);
+  L.off_copy = round_up(L.off_raw + kNRaw * kStageRows * L.raw_bytes, 128u);
+  L.off_part = round_up(L.off_copy + kStageRows * 4u * cw * 4u, 128u);
+  L.zero_word = 2u * slots * psw;
+  L.total = L.off_part + (2u * slots + 1u) * psw * 4u;
+  return L;
+}
+
+__device__ __forceinline__ void sts_v2(uint32_t addr, uint32_t a, uint32_t b) {
+  asm volatile("st.shared.v2.b32 [%0], {%1, %2};" ::"r"(addr), "r"(a), "r"(b)
+               : "memory");
+}
+
+__device__ __forceinline__ uint2 lds_v2(uint32_t addr) {
+  uint2 v;
+  asm volatile("ld.shared.v2.b32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "r"(addr));
+  return v;
+}
+
+// Issue one stage into `slot`: lane r < nrows copies row r, lane 0 also the
+// stage table.  Every lane of the warp arrives once.
+__device__ __forceinline__ void shared_issue(const ProblemDesc &P, const GroupDesc &G,
+                                             const SharedStage *stage, uint32_t slot,
+                                             uint32_t t0, const SharedLayout &L,
+                                             uint8_t *smem, int lane) {
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem) + slot;
+  const uint32_t nrows = stage->nrows;
+  const uint32_t tbytes = stage->table_bytes;
+  uint32_t bytes = 0;
+  const uint8_t *src = nullptr;
+  if ((uint32_t)lane < nrows && P.tma) {
+    const uint32_t bmin = stage->bmin[stage->row_sub[lane]];
+    const EntryDesc E = P.entries[G.entry_begin + stage->row_first + lane];
+    const uint32_t a = align_samples(P.bits);
+    const uint32_t ws = (t0 + bmin) / a * a;
+    const uint64_t boff = (uint64_t)ws * P.bits / 8u;
+    const uint64_t avail = P.row_bytes - boff;
+    bytes = avail < L.raw_bytes ? static_cast<uint32_t>(avail) : L.raw_bytes;
+    src = P.in + E.row_offset + boff;
+  }
+  const uint32_t tx = bytes + (lane == 0 ? tbytes : 0u);
+  if (tx) mbar_arrive_expect_tx(bar, tx);
+  else mbar_arrive(bar);
+  if (lane == 0)
+    bulk_g2s(smem + L.off_table + slot * P.table_bytes, P.pool + stage->pool, tbytes, bar);
+  if (bytes)
+    bulk_g2s(smem + L.off_raw + (slot * kStageRows + lane) * L.raw_bytes, src, bytes, bar);
+}
+
+// Computes one tile (TY * ND DMs x 64 * NW samples); returns false if the CTA
+// must stop (timeout).  `sc` counts the CTA's stages (mbarrier phases).
+template <int NW, int ND, int TY>
+__device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, const GroupDesc &G,
+                                             uint32_t dtile, uint32_t ttile, uint8_t *smem,
+                                             const SharedLayout &L, uint32_t &sc) {
+  constexpr int kTileT = 64 * NW;
+  constexpr int kTileD = TY * ND;
+  constexpr uint32_t kAhead = kNRaw - 1;
+  // Row expansion: warps per row and rows per pass.
+  constexpr int kRowWarps = TY >= kStageRows ? TY / kStageRows : 1;
+  constexpr int kRowStep = TY >= kStageRows ? kStageRows : TY;
+  const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+  const uint32_t t0 = ttile * kTileT;
+  const uint32_t sbeg = P.tile_stage[dtile];
+  const uint32_t nst = P.tile_stage[dtile + 1] - sbeg;
+  const uint32_t one = P.mul_hi8 >> 24;  // 1, unknown to the compiler
+  const uint32_t cw = P.cw, psw = P.psw;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
+  uint32_t *copy = reinterpret_cast<uint32_t *>(smem + L.off_copy);
+  const uint32_t copy_s = smem_addr(copy);
+  const uint32_t part_s = smem_addr(smem + L.off_part);
+
+  if (ty == 0) {
+    const uint32_t pro = nst < kAhead ? nst : kAhead;
+    for (uint32_t s = 0; s < pro; ++s)
+      shared_issue(P, G, P.stages + sbeg + s, (sc + s) % kNRaw, t0, L, smem, tx);
+  }
+
+  uint32_t acc[ND][NW], tot[ND][NW][2];
+#pragma unroll
+  for (int j = 0; j < ND; ++j)
+#pragma unroll
+    for (int i = 0; i < NW; ++i) acc[j][i] = tot[j][i][0] = tot[j][i][1] = 0;
+  uint32_t since = 0;
+
+  auto flush = [&]() {
+#pragma unroll
+    for (int j = 0; j < ND; ++j)
+#pragma unroll
+      for (int i = 0; i < NW; ++i) {
+        tot[j][i][0] += acc[j][i] & 0xFFFFu;
+        tot[j][i][1] += acc[j][i] >> 16;
+        acc[j][i] = 0;
+      }
+  };
+  auto abort = [&](uint32_t s) {
+    if (tid == 0) atomicOr(P.status, kStatusTimeout);
+    for (uint32_t u = s; u < nst && u < s + kAhead; ++u)
+      (void)mbar_wait(bars + (sc + u) % kNRaw, ((sc + u) / kNRaw) & 1u, kDrainNs);
+    return false;
+  };
+
+  for (uint32_t s = 0; s < nst; ++s) {
+    const uint32_t gs = sc + s, slot = gs % kNRaw;
+    const bool ok = mbar_wait(bars + slot, (gs / kNRaw) & 1u, kWaitNs);
+    const uint16_t *tb =
+        reinterpret_cast<const uint16_t *>(smem + L.off_table + slot * P.table_bytes);
+    uint8_t *rs = smem + L.off_raw + slot * kStageRows * L.raw_bytes;
+    const uint32_t a = align_samples(P.bits);
+    if (!P.tma) {
+      // Rows not 16-byte aligned: the CTA copies them (the table came by a
+      // bulk copy and is valid once every thread saw its wait succeed).
+      if (__syncthreads_or(!ok)) return abort(s);
+      const uint32_t rf = P.stages[sbeg + s].row_first;
+      for (uint32_t r = ty; r < tb[1]; r += TY) {
+        const uint32_t k = (r >= tb[8 + 4 + 2]) + (r >= tb[8 + 8 + 2]) + (r >= tb[8 + 12 + 2]);
+        const uint32_t bm = tb[8 + 4 * k] | ((uint32_t)tb[8 + 4 * k + 1] << 16);
+        const uint64_t boff = (uint64_t)((t0 + bm) / a * a) * P.bits / 8u;
+        const uint8_t *src = P.in + P.entries[G.entry_begin + rf + r].row_offset;
+        uint8_t *dst = rs + r * L.raw_bytes;
+        for (uint32_t b = tx; b < L.raw_bytes; b += 32)
+          dst[b] = (boff + b < P.row_bytes) ? src[boff + b] : 0;
+      }
+      __syncthreads();
+    }
+    {
+      // Expand the rows to bytes in four copies: copy m word k of row r =
+      // window samples 4k + m .. 4k + m + 3 from its subgroup's series
+      // origin t0 + bmin.  Values read before the CTA agrees that the wait
+      // succeeded are clamped so that no access leaves its buffer.
+      const uint32_t nrows = tb[1] < (uint32_t)kStageRows ? tb[1] : (uint32_t)kStageRows;
+      for (uint32_t r = (TY >= kStageRows ? ty % kStageRows : ty); r < nrows; r += kRowStep) {
+        const uint32_t k = (r >= tb[8 + 4 + 2]) + (r >= tb[8 + 8 + 2]) + (r >= tb[8 + 12 + 2]);
+        const uint32_t bm = tb[8 + 4 * k] | ((uint32_t)tb[8 + 4 * k + 1] << 16);
+        const uint32_t xw = ((t0 + bm) % a) >> 2;
+        const uint8_t *row = rs + r * L.raw_bytes;
+        uint32_t *dst = copy + r * 4u * cw;
+        const uint32_t k0 = 2u * (tx + 32u * (TY >= kStageRows ? ty / kStageRows : 0));
+        for (uint32_t kk = k0; kk < cw; kk += 64u * kRowWarps) {
+          uint32_t w0, w1, w2;
+          if (P.bits == 8) {
+            const uint32_t *r32 = reinterpret_cast<const uint32_t *>(row) + xw + kk;
+            w0 = r32[0];
+            w1 = r32[1];
+            w2 = r32[2];
+          } else {
+            w0 = expand_word(row, xw + kk, P.bits);
+            w1 = expand_word(row, xw + kk + 1, P.bits);
+            w2 = expand_word(row, xw + kk + 2, P.bits);
+          }
+          *reinterpret_cast<uint2 *>(dst + kk) = make_uint2(w0, w1);
+          *reinterpret_cast<uint2 *>(dst + cw + kk) =
+              make_uint2(__funnelshift_r(w0, w1, 8), __funnelshift_r(w1, w2, 8));
+          *reinterpret_cast<uint2 *>(dst + 2 * cw + kk) =
+              make_uint2(__funnelshift_r(w0, w1, 16), __funnelshift_r(w1, w2, 16));
+          *reinterpret_cast<uint2 *>(dst + 3 * cw + kk) =
+              make_uint2(__funnelshift_r(w0, w1, 24), __funnelshift_r(w1, w2, 24));
+        }
+      }
+    }
+    if (__syncthreads_or(!ok)) return abort(s);
+    // Every thread is past the previous stage: its slot takes stage s + kAhead.
+    if (ty == 0 && s + kAhead < nst)
+      shared_issue(P, G, P.stages + sbeg + s + kAhead, (gs + kAhead) % kNRaw, t0, L, smem,
+                   tx);
+
+    // Phase A: item = (subgroup, chunk of 31 groups of 4 samples); lane 31
+    // computes the next chunk's first group for lane 30's shifted copy.
+    const uint32_t nitems = tb[2];
+    for (uint32_t it = ty; it < nitems; it += TY) {
+      const uint32_t item = tb[kTabItems + it];
+      const uint16_t *prog = tb + tb[8 + 4 * (item >> 8) + 3];
+      const uint32_t n = prog[0], nv = prog[1], ng = prog[2];
+      uint32_t dst = prog[3];
+      const uint32_t g = (item & 0xFFu) * 31u + tx;
+      const bool act = g < ng;
+      const uint32_t gb = copy_s + 4u * g;
+      uint32_t lo = 0, hi = 0;
+      if (act) {
+        const uint4 o = *reinterpret_cast<const uint4 *>(prog + 8);
+        const uint32_t off[kSharedRows] = {o.x & 0xFFFFu, o.x >> 16, o.y & 0xFFFFu, o.y >> 16,
+                                           o.z & 0xFFFFu, o.z >> 16, o.w & 0xFFFFu, o.w >> 16};
+        if (n == (uint32_t)kSharedRows) {
+#pragma unroll
+          for (int e = 0; e < kSharedRows; ++e) {
+            const uint32_t w = lds_u32(gb + 4u * off[e]);
+            lo = mad_lo(__byte_perm(w, 0, 0x4140), one, lo);
+            hi = mad_lo(__byte_perm(w, 0, 0x4342), one, hi);
+          }
+        } else {
+#pragma unroll
+          for (int e = 0; e < kSharedRows; ++e) {
+            if ((uint32_t)e < n) {
+              const uint32_t w = lds_u32(gb + 4u * off[e]);
+              lo = mad_lo(__byte_perm(w, 0, 0x4140), one, lo);
+              hi = mad_lo(__byte_perm(w, 0, 0x4342), one, hi);
+            }
+          }
+        }
+      }
+      const uint32_t *chg = reinterpret_cast<const uint32_t *>(prog + 16);
+      for (uint32_t v = 0;;) {
+        // lo = (P[4g], P[4g+1]), hi = (P[4g+2], P[4g+3]) as 16-bit lanes.
+        const uint32_t nlo = __shfl_down_sync(0xffffffffu, lo, 1);
+        if (tx < 31 && act) {
+          const uint32_t pv = part_s + 4u * dst + 8u * g;
+          sts_v2(pv, lo, hi);
+          sts_v2(pv + 4u * psw, __byte_perm(lo, hi, 0x5432), __byte_perm(hi, nlo, 0x5432));
+        }
+        if (++v >= nv) break;
+        const uint32_t hd = *chg++;
+        dst = hd >> 16;
+        for (uint32_t q = hd & 0xFFFFu; q; --q) {
+          const uint32_t on = *chg++;
+          if (act) {
+            const uint32_t wo = lds_u32(gb + 4u * (on & 0xFFFFu));
+            const uint32_t wn = lds_u32(gb + 4u * (on >> 16));
+            lo = lo - __byte_perm(wo, 0, 0x4140) + __byte_perm(wn, 0, 0x4140);
+            hi = hi - __byte_perm(wo, 0, 0x4342) + __byte_perm(wn, 0, 0x4342);
+          }
+        }
+      }
+    }
+    __syncthreads();
+
+    // Phase B: each DM adds kSubMax series (copy base & 1, word base >> 1).
+    if (since + (uint32_t)kSubMax > kLaneSeries) {
+      flush();
+      since = 0;
+    }
+    since += kSubMax;
+    const uint16_t *offb = tb + kTabSeries + ty * ND * kSubMax;
+    const uint32_t pb = part_s + 4u * tx;
+#pragma unroll
+    for (int j = 0; j < ND; ++j) {
+      const uint2 oo = *reinterpret_cast<const uint2 *>(offb + kSubMax * j);
+      const uint32_t a0 = pb + 4u * (oo.x & 0xFFFFu), a1 = pb + 4u * (oo.x >> 16);
+      const uint32_t a2 = pb + 4u * (oo.y & 0xFFFFu), a3 = pb + 4u * (oo.y >> 16);
+#pragma unroll
+      for (int i = 0; i < NW; ++i) {
+        acc[j][i] += lds_u32(a0 + 128u * i) + lds_u32(a1 + 128u * i);
+        acc[j][i] += lds_u32(a2 + 128u * i) + lds_u32(a3 + 128u * i);
+      }
+    }
+  }
+  sc += nst;
+  flush();
+
+#pragma unroll
+  for (int j = 0; j < ND; ++j) {
+    const uint32_t d = dtile * kTileD + ty * ND + j;
+    if (d >= P.nr_dms) continue;
+    float *orow = P.out + G.out_offset + (uint64_t)d * P.out_dm_stride;
+#pragma unroll
+    for (int i = 0; i < NW; ++i) {
+      const uint32_t t = t0 + 2u * (tx + 32u * i);
+      const float v0 = (float)tot[j][i][0], v1 = (float)tot[j][i][1];
+      if (P.out_vec4 && t + 1u < P.nr_samples) {
+        *reinterpret_cast<float2 *>(orow + t) = make_float2(v0, v1);
+      } else {
+        if (t < P.nr_samples) orow[t] = v0;
+        if (t + 1u < P.nr_samples) orow[t + 1] = v1;
+      }
+    }
+  }
+  return true;
+}
+
+}  // namespace dd

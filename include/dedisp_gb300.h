@@ -275,6 +275,11 @@ dd_status dd_plan_check(dd_plan *plan, void *stream);
 dd_status dd_plan_launches(const dd_plan *plan, uint32_t *launches);
 /* The configuration the plan runs with. */
 dd_status dd_plan_get_conf(const dd_plan *plan, dd_conf *conf);
+/* Integer adds one dd_plan_run performs, tile padding included: rows x DMs x
+ * samples for the direct-sum kernels; partial sums plus series adds for the
+ * shared-partial-sum kernels (configurations with items_d2 = 8), which reach
+ * the same sums with fewer adds.  No reference counterpart. */
+dd_status dd_plan_adds(const dd_plan *plan, uint64_t *adds);
 dd_status dd_plan_destroy(dd_plan *plan);
 
 /* ---- batches: many beams in one persistent launch ------------------------ */

@@ -1,0 +1,158 @@
+"""The shared-partial-sum kernels (configurations with items_d2 = 8) on the GPU.
+
+They reach the direct sum through partial sums shared by DMs with equal
+relative delays (exact integer arithmetic), so every case must equal the
+oracle, and the direct kernels, bit for bit: sub-byte and 8-bit input, ragged
+DM and time tiles, several beams with a mapping, unaligned rows (no bulk
+copies), large DM steps (short subgroups), all-zapped, and saturated input
+(every 16-bit lane at its largest before a flush).
+"""
+import numpy as np
+import pytest
+
+import dedispersion_gb300 as dd
+from dedispersion_gb300 import synthetic as syn
+from helpers import oracle_run, single_case
+
+pytestmark = pytest.mark.gpu
+
+
+def shared_kernels():
+    ks = [k for k in dd.kernels() if k.conf.getNrItemsD2() == 8]
+    assert ks, "no shared-partial-sum configuration compiled"
+    return ks
+
+
+def run(case, kernel, torch):
+    p = dd.Plan(case.obs, dd.DD_SINGLE_STEP, case.bits, case.padding, kernel=kernel)
+    p.setShifts(case.shifts)
+    p.setZappedChannels(case.zapped)
+    p.setBeamMapping(case.mapping)
+    d_in = torch.from_numpy(case.inp).cuda()
+    d_out = torch.full((case.out_elems,), float("nan"), dtype=torch.float32, device="cuda")
+    p.run(d_in, d_out)
+    p.check()
+    adds = p.adds()
+    p.close()
+    return d_out.cpu().numpy(), adds
+
+
+def same(got, want, case):
+    g = case.valid(got).view(np.uint32)
+    w = case.valid(want).view(np.uint32)
+    bad = np.argwhere(g != w)
+    assert bad.size == 0, f"{len(bad)} mismatches, first at {bad[0]}"
+
+
+@pytest.mark.parametrize("bits", [1, 2, 4, 8])
+def test_ragged_tiles_every_configuration(gpu, oracle, bits):
+    torch = pytest.importorskip("torch")
+    case = single_case(C=256, D=100, S=1000, bits=bits, padding=128, zap=0.1, seed=bits,
+                       step=0.25, dist="uniform")
+    want = oracle_run(oracle, case)
+    for k in shared_kernels():
+        got, _ = run(case, k.index, torch)
+        same(got, want, case)
+
+
+def test_beams_and_mapping(gpu, oracle):
+    torch = pytest.importorskip("torch")
+    case = single_case(C=192, D=70, S=700, bits=8, padding=128, beams=3, sbeams=4, zap=0.2,
+                       seed=4, dist="uniform")
+    want = oracle_run(oracle, case)
+    for k in shared_kernels():
+        got, _ = run(case, k.index, torch)
+        same(got, want, case)
+
+
+def test_unaligned_rows_without_bulk_copies(gpu, oracle):
+    torch = pytest.importorskip("torch")
+    # padding 0 and an odd dispersed length: rows are not 16-byte aligned
+    case = single_case(C=96, D=40, S=300, bits=8, padding=0, zap=0.1, seed=5, extra=3,
+                       dist="uniform")
+    assert dd.layout(case.obs, dd.DD_SINGLE_STEP, 8, 0).input_row_bytes % 16 != 0
+    want = oracle_run(oracle, case)
+    for k in shared_kernels():
+        got, _ = run(case, k.index, torch)
+        same(got, want, case)
+
+
+def test_large_dm_step_cuts_subgroups(gpu, oracle):
+    torch = pytest.importorskip("torch")
+    # 4 MHz channels from 400 MHz: relative delays within eight channels pass
+    # the limit at high DMs and subgroups shrink (to ~3.6 rows on average)
+    case = single_case(C=64, D=256, S=512, bits=8, padding=128, zap=0.0, seed=6, step=0.012,
+                       fmin=400.0, bw=4.0, dist="uniform")
+    want = oracle_run(oracle, case)
+    for k in shared_kernels():
+        got, adds = run(case, k.index, torch)
+        same(got, want, case)
+        assert adds > 0
+
+
+def test_too_large_spread_is_rejected(gpu):
+    """A DM tile whose delays spread beyond the 16-bit table offsets is
+    refused with DD_ERR_UNSUPPORTED-style errors at run time, not computed."""
+    case = single_case(C=128, D=64, S=512, bits=8, padding=128, zap=0.0, seed=6, step=8.0,
+                       fmin=300.0, bw=1.0)
+    k = shared_kernels()[0]
+    p = dd.Plan(case.obs, dd.DD_SINGLE_STEP, 8, 128, kernel=k.index)
+    p.setShifts(case.shifts)
+    p.setZappedChannels(case.zapped)
+    p.setBeamMapping(case.mapping)
+    with pytest.raises(dd.DedispersionError, match="too large"):
+        p.adds()
+    p.close()
+
+
+def test_all_zapped_is_zero(gpu):
+    torch = pytest.importorskip("torch")
+    case = single_case(C=64, D=32, S=256, bits=8, padding=128, zap=1.0, seed=7)
+    assert (case.zapped[:64] != 0).all()
+    for k in shared_kernels():
+        got, adds = run(case, k.index, torch)
+        assert (case.valid(got) == 0).all()
+        assert adds == 0
+
+
+def test_saturated_input_exact(gpu):
+    """Every sample 255: each output is 255 x live channels; with 1459+ rows
+    every 16-bit lane reaches 32 x 2040 before its flush."""
+    torch = pytest.importorskip("torch")
+    case = single_case(C=1536, D=64, S=512, bits=8, padding=128, zap=0.05, seed=8,
+                       dist="constant", mean=255.0, fmin=1220.0, step=0.2, tsamp=81.92e-6)
+    live = int((case.zapped[:1536] == 0).sum())
+    for k in shared_kernels():
+        got, _ = run(case, k.index, torch)
+        assert (case.valid(got) == np.float32(255 * live)).all()
+
+
+def test_full_workload_equals_direct_kernel(gpu):
+    """1536 ch x 2048 DM x 24576 samples, 8-bit: the default shared plan and
+    the direct kernel agree bit for bit (the direct kernel is checked against
+    the oracle at this size in test_gpu_large.py), and the shared plan does
+    fewer than half the adds."""
+    torch = pytest.importorskip("torch")
+    obs = syn.large_observation(128)
+    shifts = dd.getShifts(obs, 128)
+    zapped = syn.zapped_mask(1536, 0.05, 7, 128)
+    mapping = syn.identity_mapping(obs, 128)
+    inp = syn.make_input(obs, 8, 128, seed=1, mean=128.0, sigma=20.0, pulses=20, shifts=shifts)
+    lay = dd.layout(obs, dd.DD_SINGLE_STEP, 8, 128, shifts)
+    d_in = torch.from_numpy(inp).cuda()
+    outs, adds = [], []
+    direct = next(k for k in dd.kernels() if k.elem_bits == 8 and k.conf.getNrItemsD2() == 1)
+    for k in [direct] + shared_kernels():
+        p = dd.Plan(obs, dd.DD_SINGLE_STEP, 8, 128, kernel=k.index)
+        p.setShifts(shifts)
+        p.setZappedChannels(zapped)
+        p.setBeamMapping(mapping)
+        d_out = torch.empty(lay.output_bytes // 4, dtype=torch.float32, device="cuda")
+        p.run(d_in, d_out)
+        p.check()
+        outs.append(d_out.view(-1, lay.output_row_elems)[:, :24576].cpu().numpy())
+        adds.append(p.adds())
+        p.close()
+    for o in outs[1:]:
+        assert np.array_equal(o.view(np.uint32), outs[0].view(np.uint32))
+    assert min(adds[1:]) < adds[0] / 2
