@@ -20,6 +20,7 @@
 
 #include "../../include/dedisp_gb300.h"
 #include "dd_internal.h"
+#include "dd_shared.cuh"
 #include "dd_shared_plan.h"
 
 namespace {
@@ -251,10 +252,11 @@ struct dd_plan {
   bool use_delay_tables = false;
   // Shared-partial-sum tables (kFamilyShared8 only).
   dd::SharedTables shared;
-  dd::SharedStage *d_stages = nullptr;
+  std::vector<uint4> stage_rows;  // [group][stage][32] row slots
+  uint4 *d_stage_rows = nullptr;
   uint32_t *d_tile_stage = nullptr;
   uint16_t *d_pool = nullptr;
-  size_t cap_stages = 0, cap_tile_stage = 0, cap_pool = 0;
+  size_t cap_stage_rows = 0, cap_tile_stage = 0, cap_pool = 0;
   std::string invalid;  // why the tables are not usable (empty when ready)
   bool ready = false;
 };
@@ -448,7 +450,7 @@ dd_status rebuild(dd_plan *p) {
   if (p->use_delay_tables) {
     if (p->delay_rel.size() > p->cap_delay_rel) {
       if (p->d_delay_rel) cudaFree(p->d_delay_rel);
-    if (p->d_stages) cudaFree(p->d_stages);
+    if (p->d_stage_rows) cudaFree(p->d_stage_rows);
     if (p->d_tile_stage) cudaFree(p->d_tile_stage);
     if (p->d_pool) cudaFree(p->d_pool);
       p->d_delay_rel = nullptr;
@@ -474,7 +476,25 @@ dd_status rebuild(dd_plan *p) {
         DD_CUDA(cudaMemcpy(*dptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), what);
       return DD_OK;
     };
-    dd_status us = upload(&p->d_stages, &p->cap_stages, p->shared.stages, "upload stage table");
+    // Row slots of every stage for every group: the row's byte offset, its
+    // subgroup's window start, the stage table's pool index.
+    const std::vector<dd::SharedStage> &sts = p->shared.stages;
+    p->stage_rows.assign((size_t)p->nr_groups * sts.size() * dd::kStageRows, uint4{0, 0, 0, 0});
+    for (uint32_t gi = 0; gi < p->nr_groups; gi++)
+      for (size_t si = 0; si < sts.size(); si++) {
+        uint4 *slot = &p->stage_rows[((size_t)gi * sts.size() + si) * dd::kStageRows];
+        for (uint32_t r = 0; r < (uint32_t)dd::kStageRows; r++) {
+          slot[r].w = sts[si].pool;
+          if (r >= sts[si].nrows) continue;
+          const uint64_t off =
+              p->entries[p->groups[gi].entry_begin + sts[si].row_first + r].row_offset;
+          slot[r].x = (uint32_t)(off & 0xFFFFFFFFu);
+          slot[r].y = (uint32_t)(off >> 32);
+          slot[r].z = sts[si].bmin[sts[si].row_sub[r]] | dd::kRowPresent;
+        }
+      }
+    dd_status us = upload(&p->d_stage_rows, &p->cap_stage_rows, p->stage_rows,
+                          "upload stage rows");
     if (!us) us = upload(&p->d_tile_stage, &p->cap_tile_stage, p->shared.tile_stage,
                          "upload tile stage table");
     if (!us) us = upload(&p->d_pool, &p->cap_pool, p->shared.pool, "upload stage pool");
@@ -532,7 +552,8 @@ dd_status plan_problem(const dd_plan *p, const void *d_input, float *d_output,
     P.delay_rel = p->d_delay_rel;
   }
   if (p->kinfo->family == kFamilyShared8) {
-    P.stages = p->d_stages;
+    P.stage_rows = p->d_stage_rows;
+    P.stage_count = (uint32_t)p->shared.stages.size();
     P.tile_stage = p->d_tile_stage;
     P.pool = p->d_pool;
     P.cw = p->shared.cw;
@@ -930,7 +951,7 @@ dd_status dd_plan_destroy(dd_plan *p) {
     if (p->d_entries) cudaFree(p->d_entries);
     if (p->d_status) cudaFree(p->d_status);
     if (p->d_delay_rel) cudaFree(p->d_delay_rel);
-    if (p->d_stages) cudaFree(p->d_stages);
+    if (p->d_stage_rows) cudaFree(p->d_stage_rows);
     if (p->d_tile_stage) cudaFree(p->d_tile_stage);
     if (p->d_pool) cudaFree(p->d_pool);
   }

@@ -93,7 +93,8 @@ struct ProblemDesc {
   //       = delay(r, min(d0 + j, nr_dms - 1)) - delay(r, d0)
   const uint16_t *delay_rel;
   // Shared-partial-sum family only (NULL otherwise).
-  const SharedStage *stages;    // all DM tiles' stages
+  const uint4 *stage_rows;      // [group][stage][32] row slots (dd_shared.cuh)
+  uint32_t stage_count;         // stages of one group (all DM tiles)
   const uint32_t *tile_stage;   // [tiles_d + 1]: first stage of each DM tile
   const uint16_t *pool;         // stage tables
   uint32_t cw;                  // words per shifted copy of a staged row (even)

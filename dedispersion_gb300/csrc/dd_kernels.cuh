@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(32 * TY, (TY >= 16 ? 1 : 2))
   const SharedLayout L = make_shared_layout(P.cw, P.psw, P.slots, P.table_bytes, P.bits);
   if (threadIdx.x == 0) {
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
-    for (int r = 0; r < kNRaw; ++r) mbar_init(bars + r, kSharedArrivals);
+    for (int r = 0; r < kSharedSlots; ++r) mbar_init(bars + r, blockDim.x);
     fence_mbar_init();
   }
   // The zero series that absent subgroups of a stage read.
@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(32 * TY, (TY >= 16 ? 1 : 2))
   __syncthreads();
   uint32_t g, dtile, ttile, sc = 0;
   decode_tile(P, blockIdx.x, g, dtile, ttile);
-  (void)shared8_tile<NW, ND, TY>(P, P.groups[g], dtile, ttile, smem, L, sc);
+  (void)shared8_tile<NW, ND, TY>(P, g, P.groups[g], dtile, ttile, smem, L, sc);
 }
 
 template <int NW, int NDT, int TY, int CH, int VAR>

@@ -17,14 +17,16 @@
 // Phase A walks each subgroup's vectors in a chain chosen on the host so
 // that consecutive vectors differ in few rows: the first is summed over its
 // rows, each next one is the previous minus the rows that moved plus their
-// new samples.  Integer addition is exact and every intermediate value is a
+// new samples.  The chain is cut in two halves that a lane runs side by
+// side (two independent dependency chains per lane).  Integer addition is exact and every intermediate value is a
 // sum of samples (non-negative), so the result equals the direct form's bit
 // for bit (8-bit rows: P <= 8 * 255, output < 2^24).  On the 1536-channel,
 // 2048-DM table the adds per DM-sample drop from 1459 to about 320.
 //
 // A pipeline stage holds up to kSubMax subgroups (kStageRows rows).  Per
-// stage: the rows arrive by bulk copies (one per row, plus the stage table)
-// in one of kNRaw slots; the CTA expands them into four byte-shifted copies
+// stage: the rows and the stage table arrive by 16-byte asynchronous copies
+// (every thread copies a share, completion counted on the slot's mbarrier)
+// in one of kSharedSlots slots; the CTA expands them into four byte-shifted copies
 // (any window read is one aligned 32-bit load); warps run the chains of
 // (subgroup, 31-group chunk) work items, writing each series in two copies
 // shifted by one sample (a read at any offset is aligned loads of two 16-bit
@@ -41,8 +43,8 @@
 namespace dd {
 
 constexpr int kSubMax = 4;                              // subgroups per stage
+constexpr int kSharedSlots = 3;                         // stages staged at once
 constexpr int kStageRows = kSubMax * kSharedRows;       // rows per stage
-constexpr uint32_t kSharedArrivals = 32;                // lanes of the issuing warp
 constexpr uint32_t kLaneSeries = 32;                    // series per 16-bit lane (32 * 2040 < 2^16)
 constexpr uint32_t kItemsMax = 32;                      // phase-A items per stage
 // Stage table (u16 units, in shared memory):
@@ -50,8 +52,10 @@ constexpr uint32_t kItemsMax = 32;                      // phase-A items per sta
 //   [8 + 4k] bmin_k lo, [+1] bmin_k hi, [+2] first row of k, [+3] program of k
 //   [kTabItems ..)         items: subgroup << 8 | chunk
 //   [kTabSeries ..)        per DM of the tile, kSubMax series offsets (words)
-//   programs, each 8-aligned: [n, nv, ng, dst0, 0 x4], 8 row offsets, then
-//   per next vector: u32 (h | dst << 16) and h x u32 (old | new << 16)
+//   programs, each 8-aligned: [n, ng, nA, nB, dstA, dstB (0xFFFF: no B), 0, 0],
+//   8 row offsets of chain A's first vector, 8 of chain B's, then nA and nB
+//   micro-ops of 4 u16: (old offset, new offset, dst after this one or
+//   0xFFFF, 0)
 constexpr uint32_t kTabItems = 8 + 4 * kSubMax;
 constexpr uint32_t kTabSeries = kTabItems + kItemsMax;
 
@@ -60,7 +64,7 @@ struct SharedLayout {
   uint32_t off_table, off_raw, off_copy, off_part, zero_word, total;
 };
 
-// Shared memory of one CTA: mbarriers, kNRaw stage tables, kNRaw x
+// Shared memory of one CTA: mbarriers, kSharedSlots stage tables and x
 // kStageRows raw rows, the shifted copies of one stage's rows, `slots`
 // partial-sum series (two copies each) and one zero series.  Host and device
 // use this one formula.
@@ -72,8 +76,8 @@ __host__ __device__ inline SharedLayout make_shared_layout(uint32_t cw, uint32_t
   const uint32_t win = 4u * cw + 8u + align_samples(bits);  // samples per row
   L.raw_bytes = round_up(win * bits / 8u, 16u);
   L.off_table = 128;
-  L.off_raw = round_up(L.off_table + kNRaw * table_bytes, 128u);
-  L.off_copy = round_up(L.off_raw + kNRaw * kStageRows * L.raw_bytes, 128u);
+  L.off_raw = round_up(L.off_table + kSharedSlots * table_bytes, 128u);
+  L.off_copy = round_up(L.off_raw + kSharedSlots * kStageRows * L.raw_bytes, 128u);
   L.off_part = round_up(L.off_copy + kStageRows * 4u * cw * 4u, 128u);
   L.zero_word = 2u * slots * psw;
   L.total = L.off_part + (2u * slots + 1u) * psw * 4u;
@@ -91,45 +95,65 @@ __device__ __forceinline__ uint2 lds_v2(uint32_t addr) {
   return v;
 }
 
-// Issue one stage into `slot`: lane r < nrows copies row r, lane 0 also the
-// stage table.  Every lane of the warp arrives once.
-__device__ __forceinline__ void shared_issue(const ProblemDesc &P, const GroupDesc &G,
-                                             const SharedStage *stage, uint32_t slot,
-                                             uint32_t t0, const SharedLayout &L,
-                                             uint8_t *smem, int lane) {
-  uint64_t *bar = reinterpret_cast<uint64_t *>(smem) + slot;
-  const uint32_t nrows = stage->nrows;
-  const uint32_t tbytes = stage->table_bytes;
-  uint32_t bytes = 0;
-  const uint8_t *src = nullptr;
-  if ((uint32_t)lane < nrows && P.tma) {
-    const uint32_t bmin = stage->bmin[stage->row_sub[lane]];
-    const EntryDesc E = P.entries[G.entry_begin + stage->row_first + lane];
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src),
+               "r"(src_bytes)
+               : "memory");
+}
+
+// Arrive on `bar` once every cp.async this thread issued before has landed.
+__device__ __forceinline__ void cp_async_arrive(uint64_t *bar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_addr(bar))
+               : "memory");
+}
+
+// Row slot r of a stage (host-built, per group): x, y = byte offset of the
+// row in the input, z = its subgroup's window start | kRowPresent, w = u16
+// index of the stage table in the pool.
+constexpr uint32_t kRowPresent = 0x80000000u;
+
+__device__ __forceinline__ uint4 shared_row_info(const ProblemDesc &P, uint32_t g,
+                                                 uint32_t stage, uint32_t r) {
+  return __ldg(P.stage_rows + ((size_t)g * P.stage_count + stage) * kStageRows + r);
+}
+
+// Copies one stage into `slot` with 16-byte asynchronous copies (the
+// vectorised staging path; one bulk copy per ~500-byte row costs more): 16
+// threads per row slot, thread tid also copies 16 bytes of the stage table,
+// then every thread arrives on the slot's mbarrier when its copies land.
+// `info` is the thread's row slot (row tid / 16).
+__device__ __forceinline__ void shared_copy(const ProblemDesc &P, const uint4 &info,
+                                            uint32_t slot, uint32_t t0, const SharedLayout &L,
+                                            uint8_t *smem, int tid) {
+  const uint32_t r = (uint32_t)tid >> 4, c0 = (uint32_t)tid & 15u;
+  if ((info.z & kRowPresent) && P.tma) {
     const uint32_t a = align_samples(P.bits);
-    const uint32_t ws = (t0 + bmin) / a * a;
+    const uint32_t ws = (t0 + (info.z & ~kRowPresent)) / a * a;
     const uint64_t boff = (uint64_t)ws * P.bits / 8u;
     const uint64_t avail = P.row_bytes - boff;
-    bytes = avail < L.raw_bytes ? static_cast<uint32_t>(avail) : L.raw_bytes;
-    src = P.in + E.row_offset + boff;
+    const uint8_t *src = P.in + (((uint64_t)info.y << 32) | info.x) + boff;
+    const uint32_t dst = smem_addr(smem + L.off_raw + (slot * kStageRows + r) * L.raw_bytes);
+    for (uint32_t b = 16u * c0; b < L.raw_bytes; b += 256u) {
+      const uint32_t n = avail > b ? (avail - b < 16u ? (uint32_t)(avail - b) : 16u) : 0u;
+      cp_async16(dst + b, n ? src + b : src, n);
+    }
   }
-  const uint32_t tx = bytes + (lane == 0 ? tbytes : 0u);
-  if (tx) mbar_arrive_expect_tx(bar, tx);
-  else mbar_arrive(bar);
-  if (lane == 0)
-    bulk_g2s(smem + L.off_table + slot * P.table_bytes, P.pool + stage->pool, tbytes, bar);
-  if (bytes)
-    bulk_g2s(smem + L.off_raw + (slot * kStageRows + lane) * L.raw_bytes, src, bytes, bar);
+  if (16u * (uint32_t)tid < P.table_bytes)
+    cp_async16(smem_addr(smem + L.off_table + slot * P.table_bytes) + 16u * tid,
+               P.pool + info.w + 8u * tid, 16u);
+  cp_async_arrive(reinterpret_cast<uint64_t *>(smem) + slot);
 }
 
 // Computes one tile (TY * ND DMs x 64 * NW samples); returns false if the CTA
 // must stop (timeout).  `sc` counts the CTA's stages (mbarrier phases).
 template <int NW, int ND, int TY>
-__device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, const GroupDesc &G,
-                                             uint32_t dtile, uint32_t ttile, uint8_t *smem,
-                                             const SharedLayout &L, uint32_t &sc) {
+__device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_index,
+                                             const GroupDesc &G, uint32_t dtile, uint32_t ttile,
+                                             uint8_t *smem, const SharedLayout &L, uint32_t &sc) {
+  static_assert(32 * TY == 16 * kStageRows, "16 threads per row slot");
   constexpr int kTileT = 64 * NW;
   constexpr int kTileD = TY * ND;
-  constexpr uint32_t kAhead = kNRaw - 1;
+  constexpr uint32_t kAhead = kSharedSlots - 1;
   // Row expansion: warps per row and rows per pass.
   constexpr int kRowWarps = TY >= kStageRows ? TY / kStageRows : 1;
   constexpr int kRowStep = TY >= kStageRows ? kStageRows : TY;
@@ -144,11 +168,17 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, const GroupDe
   const uint32_t copy_s = smem_addr(copy);
   const uint32_t part_s = smem_addr(smem + L.off_part);
 
-  if (ty == 0) {
+  // Every thread copies a share of each stage; `next` is its row slot of the
+  // next stage to copy, loaded one stage ahead.
+  const uint32_t myrow = (uint32_t)tid >> 4;
+  {
     const uint32_t pro = nst < kAhead ? nst : kAhead;
     for (uint32_t s = 0; s < pro; ++s)
-      shared_issue(P, G, P.stages + sbeg + s, (sc + s) % kNRaw, t0, L, smem, tx);
+      shared_copy(P, shared_row_info(P, g_index, sbeg + s, myrow), (sc + s) % kSharedSlots, t0,
+                  L, smem, tid);
   }
+  uint4 next = make_uint4(0, 0, 0, 0);
+  if (kAhead < nst) next = shared_row_info(P, g_index, sbeg + kAhead, myrow);
 
   uint32_t acc[ND][NW], tot[ND][NW][2];
 #pragma unroll
@@ -170,27 +200,27 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, const GroupDe
   auto abort = [&](uint32_t s) {
     if (tid == 0) atomicOr(P.status, kStatusTimeout);
     for (uint32_t u = s; u < nst && u < s + kAhead; ++u)
-      (void)mbar_wait(bars + (sc + u) % kNRaw, ((sc + u) / kNRaw) & 1u, kDrainNs);
+      (void)mbar_wait(bars + (sc + u) % kSharedSlots, ((sc + u) / kSharedSlots) & 1u, kDrainNs);
     return false;
   };
 
   for (uint32_t s = 0; s < nst; ++s) {
-    const uint32_t gs = sc + s, slot = gs % kNRaw;
-    const bool ok = mbar_wait(bars + slot, (gs / kNRaw) & 1u, kWaitNs);
+    const uint32_t gs = sc + s, slot = gs % kSharedSlots;
+    const bool ok = mbar_wait(bars + slot, (gs / kSharedSlots) & 1u, kWaitNs);
     const uint16_t *tb =
         reinterpret_cast<const uint16_t *>(smem + L.off_table + slot * P.table_bytes);
     uint8_t *rs = smem + L.off_raw + slot * kStageRows * L.raw_bytes;
     const uint32_t a = align_samples(P.bits);
     if (!P.tma) {
-      // Rows not 16-byte aligned: the CTA copies them (the table came by a
-      // bulk copy and is valid once every thread saw its wait succeed).
+      // Rows not 16-byte aligned: the CTA copies them (the table came by
+      // asynchronous copies and is valid once every thread saw its wait
+      // succeed).
       if (__syncthreads_or(!ok)) return abort(s);
-      const uint32_t rf = P.stages[sbeg + s].row_first;
       for (uint32_t r = ty; r < tb[1]; r += TY) {
-        const uint32_t k = (r >= tb[8 + 4 + 2]) + (r >= tb[8 + 8 + 2]) + (r >= tb[8 + 12 + 2]);
-        const uint32_t bm = tb[8 + 4 * k] | ((uint32_t)tb[8 + 4 * k + 1] << 16);
+        const uint4 info = shared_row_info(P, g_index, sbeg + s, r);
+        const uint32_t bm = info.z & ~kRowPresent;
         const uint64_t boff = (uint64_t)((t0 + bm) / a * a) * P.bits / 8u;
-        const uint8_t *src = P.in + P.entries[G.entry_begin + rf + r].row_offset;
+        const uint8_t *src = P.in + (((uint64_t)info.y << 32) | info.x);
         uint8_t *dst = rs + r * L.raw_bytes;
         for (uint32_t b = tx; b < L.raw_bytes; b += 32)
           dst[b] = (boff + b < P.row_bytes) ? src[boff + b] : 0;
@@ -234,65 +264,83 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, const GroupDe
     }
     if (__syncthreads_or(!ok)) return abort(s);
     // Every thread is past the previous stage: its slot takes stage s + kAhead.
-    if (ty == 0 && s + kAhead < nst)
-      shared_issue(P, G, P.stages + sbeg + s + kAhead, (gs + kAhead) % kNRaw, t0, L, smem,
-                   tx);
+    if (s + kAhead < nst) {
+      shared_copy(P, next, (gs + kAhead) % kSharedSlots, t0, L, smem, tid);
+      if (s + kAhead + 1 < nst) next = shared_row_info(P, g_index, sbeg + s + kAhead + 1, myrow);
+    }
 
     // Phase A: item = (subgroup, chunk of 31 groups of 4 samples); lane 31
-    // computes the next chunk's first group for lane 30's shifted copy.
+    // computes the next chunk's first group for lane 30's shifted copy.  Each
+    // lane runs the subgroup's two half-chains A and B side by side (two
+    // independent dependency chains), one micro-op (one moved row) of each
+    // per step.
     const uint32_t nitems = tb[2];
     for (uint32_t it = ty; it < nitems; it += TY) {
       const uint32_t item = tb[kTabItems + it];
       const uint16_t *prog = tb + tb[8 + 4 * (item >> 8) + 3];
-      const uint32_t n = prog[0], nv = prog[1], ng = prog[2];
-      uint32_t dst = prog[3];
+      const uint4 hdr = *reinterpret_cast<const uint4 *>(prog);
+      const uint32_t n = hdr.x & 0xFFFFu, ng = hdr.x >> 16;
+      const uint32_t nA = hdr.y & 0xFFFFu, nB = hdr.y >> 16;
       const uint32_t g = (item & 0xFFu) * 31u + tx;
-      const bool act = g < ng;
+      const bool act = g < ng, hasB = (hdr.z >> 16) != 0xFFFFu;
       const uint32_t gb = copy_s + 4u * g;
-      uint32_t lo = 0, hi = 0;
-      if (act) {
-        const uint4 o = *reinterpret_cast<const uint4 *>(prog + 8);
+      // lo = (P[4g], P[4g+1]), hi = (P[4g+2], P[4g+3]) as 16-bit lanes.
+      uint32_t loA = 0, hiA = 0, loB = 0, hiB = 0;
+      auto rows = [&](const uint16_t *offs, uint32_t &lo, uint32_t &hi) {
+        const uint4 o = *reinterpret_cast<const uint4 *>(offs);
         const uint32_t off[kSharedRows] = {o.x & 0xFFFFu, o.x >> 16, o.y & 0xFFFFu, o.y >> 16,
                                            o.z & 0xFFFFu, o.z >> 16, o.w & 0xFFFFu, o.w >> 16};
-        if (n == (uint32_t)kSharedRows) {
 #pragma unroll
-          for (int e = 0; e < kSharedRows; ++e) {
+        for (int e = 0; e < kSharedRows; ++e) {
+          if ((uint32_t)e < n) {
             const uint32_t w = lds_u32(gb + 4u * off[e]);
             lo = mad_lo(__byte_perm(w, 0, 0x4140), one, lo);
             hi = mad_lo(__byte_perm(w, 0, 0x4342), one, hi);
           }
-        } else {
-#pragma unroll
-          for (int e = 0; e < kSharedRows; ++e) {
-            if ((uint32_t)e < n) {
-              const uint32_t w = lds_u32(gb + 4u * off[e]);
-              lo = mad_lo(__byte_perm(w, 0, 0x4140), one, lo);
-              hi = mad_lo(__byte_perm(w, 0, 0x4342), one, hi);
-            }
-          }
         }
-      }
-      const uint32_t *chg = reinterpret_cast<const uint32_t *>(prog + 16);
-      for (uint32_t v = 0;;) {
-        // lo = (P[4g], P[4g+1]), hi = (P[4g+2], P[4g+3]) as 16-bit lanes.
+      };
+      auto store = [&](uint32_t dst, uint32_t lo, uint32_t hi) {
         const uint32_t nlo = __shfl_down_sync(0xffffffffu, lo, 1);
         if (tx < 31 && act) {
           const uint32_t pv = part_s + 4u * dst + 8u * g;
           sts_v2(pv, lo, hi);
           sts_v2(pv + 4u * psw, __byte_perm(lo, hi, 0x5432), __byte_perm(hi, nlo, 0x5432));
         }
-        if (++v >= nv) break;
-        const uint32_t hd = *chg++;
-        dst = hd >> 16;
-        for (uint32_t q = hd & 0xFFFFu; q; --q) {
-          const uint32_t on = *chg++;
-          if (act) {
-            const uint32_t wo = lds_u32(gb + 4u * (on & 0xFFFFu));
-            const uint32_t wn = lds_u32(gb + 4u * (on >> 16));
-            lo = lo - __byte_perm(wo, 0, 0x4140) + __byte_perm(wn, 0, 0x4140);
-            hi = hi - __byte_perm(wo, 0, 0x4342) + __byte_perm(wn, 0, 0x4342);
-          }
+      };
+      auto step = [&](const uint2 u, uint32_t &lo, uint32_t &hi) {
+        if (act) {
+          const uint32_t wo = lds_u32(gb + 4u * (u.x & 0xFFFFu));
+          const uint32_t wn = lds_u32(gb + 4u * (u.x >> 16));
+          lo = lo - __byte_perm(wo, 0, 0x4140) + __byte_perm(wn, 0, 0x4140);
+          hi = hi - __byte_perm(wo, 0, 0x4342) + __byte_perm(wn, 0, 0x4342);
         }
+      };
+      if (act) {
+        rows(prog + 8, loA, hiA);
+        if (hasB) rows(prog + 16, loB, hiB);
+      }
+      store(hdr.z & 0xFFFFu, loA, hiA);
+      if (hasB) store(hdr.z >> 16, loB, hiB);
+      const uint2 *ua = reinterpret_cast<const uint2 *>(prog + 24);
+      const uint2 *ub = ua + nA;
+      const uint32_t both = nA < nB ? nA : nB;
+      uint32_t i = 0;
+      for (; i < both; ++i) {
+        const uint2 a = ua[i], b = ub[i];
+        step(a, loA, hiA);
+        step(b, loB, hiB);
+        if ((a.y & 0xFFFFu) != 0xFFFFu) store(a.y & 0xFFFFu, loA, hiA);
+        if ((b.y & 0xFFFFu) != 0xFFFFu) store(b.y & 0xFFFFu, loB, hiB);
+      }
+      for (; i < nA; ++i) {
+        const uint2 a = ua[i];
+        step(a, loA, hiA);
+        if ((a.y & 0xFFFFu) != 0xFFFFu) store(a.y & 0xFFFFu, loA, hiA);
+      }
+      for (; i < nB; ++i) {
+        const uint2 b = ub[i];
+        step(b, loB, hiB);
+        if ((b.y & 0xFFFFu) != 0xFFFFu) store(b.y & 0xFFFFu, loB, hiB);
       }
     }
     __syncthreads();

@@ -189,8 +189,8 @@ std::string build_shared_tables(const KernelInfo &k, const std::vector<float> &r
       return fmt("DM spread of %llu samples per tile is too large for 16-bit copy offsets "
                  "(tile of %llu DMs); use fewer DMs per tile", spread, DB);
     // Table size bound: header, items, series offsets, and per subgroup a
-    // program of 16 + 2 * (nv - 1) * (1 + n) entries.
-    const uint32_t prog_max = kSubMax * (16 + 2 * (nv_max - 1) * (1 + kSharedRows) + 8);
+    // program of 24 + 4 * (micro-ops <= (nv - 1) * n) entries.
+    const uint32_t prog_max = kSubMax * (24 + 4 * (nv_max - 1) * kSharedRows + 8);
     const uint32_t tbytes = ((2 * (kTabSeries + kSubMax * DB + prog_max)) + 15) / 16 * 16;
     S.slots = 0;
     for (uint32_t sl = kSubMax * nv_cap; sl >= 1; sl--) {
@@ -271,25 +271,53 @@ std::string build_shared_tables(const KernelInfo &k, const std::vector<float> &r
           return (uint16_t)((rstart + e) * 4 * S.cw + (rel & 3u) * S.cw + (rel >> 2));
         };
         const uint32_t nvq = (uint32_t)s.vec.size();
+        std::vector<uint32_t> h(nvq, 0);  // rows moved from vector v - 1 to v
+        for (uint32_t v = 1; v < nvq; v++) h[v] = hamming(s.vec[v - 1], s.vec[v], s.n);
+        // Half B starts at vector m (from scratch): balance the micro-ops.
+        uint32_t m = nvq, best = UINT32_MAX;
+        if (nvq >= 2) {
+          uint32_t total = 0;
+          for (uint32_t v = 1; v < nvq; v++) total += h[v];
+          uint32_t pre = 0;  // micro-ops of A = sum h[1..m-1]
+          for (uint32_t mm = 1; mm < nvq; mm++) {
+            if (mm > 1) pre += h[mm - 1];
+            const uint32_t b = total - pre - h[mm];
+            const uint32_t cost = std::max(pre, b);
+            if (cost < best) { best = cost; m = mm; }
+          }
+        }
+        const bool hasB = m < nvq;
+        auto dst_of = [&](uint32_t v) { return (uint16_t)(2 * (slot + v) * S.psw); };
+        std::vector<uint16_t> ua, ub;
+        auto uops = [&](std::vector<uint16_t> &u, uint32_t from, uint32_t to) {
+          for (uint32_t v = from + 1; v < to; v++) {
+            uint32_t left = h[v];
+            for (uint32_t e = 0; e < s.n; e++)
+              if (s.vec[v - 1][e] != s.vec[v][e]) {
+                u.push_back(off(e, s.vec[v - 1][e]));
+                u.push_back(off(e, s.vec[v][e]));
+                u.push_back(--left == 0 ? dst_of(v) : (uint16_t)0xFFFF);
+                u.push_back(0);
+              }
+          }
+        };
+        uops(ua, 0, m);
+        if (hasB) uops(ub, m, nvq);
         tb.push_back((uint16_t)s.n);
-        tb.push_back((uint16_t)nvq);
         tb.push_back((uint16_t)ng);
-        tb.push_back((uint16_t)(2 * slot * S.psw));
-        for (int z = 0; z < 4; z++) tb.push_back(0);
+        tb.push_back((uint16_t)(ua.size() / 4));
+        tb.push_back((uint16_t)(ub.size() / 4));
+        tb.push_back(dst_of(0));
+        tb.push_back(hasB ? dst_of(m) : (uint16_t)0xFFFF);
+        tb.push_back(0);
+        tb.push_back(0);
         for (uint32_t e = 0; e < (uint32_t)kSharedRows; e++)
           tb.push_back(e < s.n ? off(e, s.vec[0][e]) : (uint16_t)0);
-        uint64_t row_ops = s.n;
-        for (uint32_t v = 1; v < nvq; v++) {
-          const uint32_t h = hamming(s.vec[v - 1], s.vec[v], s.n);
-          tb.push_back((uint16_t)h);
-          tb.push_back((uint16_t)(2 * (slot + v) * S.psw));
-          for (uint32_t e = 0; e < s.n; e++)
-            if (s.vec[v - 1][e] != s.vec[v][e]) {
-              tb.push_back(off(e, s.vec[v - 1][e]));
-              tb.push_back(off(e, s.vec[v][e]));
-            }
-          row_ops += 2 * h;
-        }
+        for (uint32_t e = 0; e < (uint32_t)kSharedRows; e++)
+          tb.push_back(hasB && e < s.n ? off(e, s.vec[m][e]) : (uint16_t)0);
+        tb.insert(tb.end(), ua.begin(), ua.end());
+        tb.insert(tb.end(), ub.begin(), ub.end());
+        const uint64_t row_ops = s.n * (hasB ? 2u : 1u) + 2 * (ua.size() + ub.size()) / 4;
         S.adds_partial += row_ops * 4 * ng;
         S.adds_series += (uint64_t)DB * T;
         slot += nvq;
@@ -310,8 +338,10 @@ std::string build_shared_tables(const KernelInfo &k, const std::vector<float> &r
   }
   if (tb_max > S.table_bytes)
     return fmt("stage table of %llu bytes exceeds its bound of %llu", tb_max, S.table_bytes);
-  // Table slots sized to the largest actual table.
+  // Table slots sized to the largest actual table; every stage copies that
+  // many bytes, so the pool ends with one table's worth of zeros.
   S.table_bytes = tb_max;
+  S.pool.insert(S.pool.end(), tb_max / 2, 0);
   S.smem = make_shared_layout(S.cw, S.psw, S.slots, tb_max, bits).total;
   return "";
 }

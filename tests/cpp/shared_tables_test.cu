@@ -137,60 +137,70 @@ int main(int argc, char **argv) {
             if (q >= nsub) return fail("item subgroup", s, it, q);
             const uint32_t pg = T16(8 + 4 * q + 3);
             if (pg % 8) return fail("program alignment", s, q, pg);
-            const uint32_t n = T16(pg), nv = T16(pg + 1), ng = T16(pg + 2);
-            uint32_t dst = T16(pg + 3);
-            uint32_t lo[32] = {0}, hi[32] = {0};
-            for (uint32_t lane = 0; lane < 32; lane++) {
-              const uint32_t g = c * 31 + lane;
-              if (g >= ng) continue;
-              for (uint32_t e = 0; e < n; e++) {
-                uint32_t w;
-                if (!rd(T16(pg + 8 + e), g, w)) return fail("copy read", s, q, e);
-                lo[lane] += prmt4140(w);
-                hi[lane] += prmt4342(w);
+            const uint32_t n = T16(pg), ng = T16(pg + 1), nA = T16(pg + 2), nB = T16(pg + 3);
+            const uint32_t dA = T16(pg + 4), dB = T16(pg + 5);
+            if (n < 1 || n > (uint32_t)kSharedRows) return fail("program rows", s, q, n);
+            // both half-chains of every lane of the chunk
+            for (uint32_t half = 0; half < 2; half++) {
+              const uint32_t d0 = half ? dB : dA;
+              if (half && d0 == 0xFFFFu) {
+                if (nB) return fail("half B without start", s, q, nB);
+                break;
               }
-              partial_ops += 4 * n;
-            }
-            size_t pc = pg + 16;
-            for (uint32_t v = 0;;) {
-              for (uint32_t lane = 0; lane < 31; lane++) {
+              uint32_t lo[32] = {0}, hi[32] = {0};
+              for (uint32_t lane = 0; lane < 32; lane++) {
                 const uint32_t g = c * 31 + lane;
                 if (g >= ng) continue;
-                const uint32_t nlo = lo[lane + 1];
-                const size_t c0 = (size_t)dst + 2 * g, c1 = c0 + psw;
-                if (dst % (2 * psw) || 2 * g + 1 >= psw || c1 + 1 >= 2 * (size_t)tab.slots * psw)
-                  return fail("series write", s, dst, g);
-                part[c0] = lo[lane];
-                part[c0 + 1] = hi[lane];
-                part[c1] = (lo[lane] >> 16) | (hi[lane] << 16);
-                part[c1 + 1] = (hi[lane] >> 16) | (nlo << 16);
-                written[c0] = written[c0 + 1] = written[c1] = 1;
-                written[c1 + 1] = g + 1 < ng ? 1 : 2;  // 2: holds a zero neighbour
-                for (uint32_t x : {lo[lane], hi[lane]})
-                  if ((x & 0xFFFF) > 8 * 255 || (x >> 16) > 8 * 255) return fail("lane range", s, g, x);
+                for (uint32_t e = 0; e < n; e++) {
+                  uint32_t w;
+                  if (!rd(T16(pg + 8 + 8 * half + e), g, w)) return fail("copy read", s, q, e);
+                  lo[lane] += prmt4140(w);
+                  hi[lane] += prmt4342(w);
+                }
+                partial_ops += 4 * n;
               }
-              if (++v >= nv) break;
-              const uint32_t h = T16(pc), nd = T16(pc + 1);
-              pc += 2;
-              dst = nd;
-              for (uint32_t qq = 0; qq < h; qq++) {
-                const uint32_t o = T16(pc), nw = T16(pc + 1);
-                pc += 2;
+              auto store = [&](uint32_t dst) {
+                for (uint32_t lane = 0; lane < 31; lane++) {
+                  const uint32_t g = c * 31 + lane;
+                  if (g >= ng) continue;
+                  const uint32_t nlo = lo[lane + 1];
+                  const size_t c0 = (size_t)dst + 2 * g, c1 = c0 + psw;
+                  if (dst % (2 * psw) || 2 * g + 1 >= psw || c1 + 1 >= 2 * (size_t)tab.slots * psw)
+                    return fail("series write", s, dst, g);
+                  part[c0] = lo[lane];
+                  part[c0 + 1] = hi[lane];
+                  part[c1] = (lo[lane] >> 16) | (hi[lane] << 16);
+                  part[c1 + 1] = (hi[lane] >> 16) | (nlo << 16);
+                  written[c0] = written[c0 + 1] = written[c1] = 1;
+                  written[c1 + 1] = g + 1 < ng ? 1 : 2;  // 2: holds a zero neighbour
+                  for (uint32_t x : {lo[lane], hi[lane]})
+                    if ((x & 0xFFFF) > 8 * 255 || (x >> 16) > 8 * 255)
+                      return fail("lane range", s, g, x);
+                }
+                return 0;
+              };
+              if (store(d0)) return 1;
+              const size_t u0 = pg + 24 + (half ? 4 * nA : 0);
+              const uint32_t nu = half ? nB : nA;
+              for (uint32_t i = 0; i < nu; i++) {
+                const uint32_t o = T16(u0 + 4 * i), nw = T16(u0 + 4 * i + 1);
+                const uint32_t dst = T16(u0 + 4 * i + 2);
                 for (uint32_t lane = 0; lane < 32; lane++) {
                   const uint32_t g = c * 31 + lane;
                   if (g >= ng) continue;
                   uint32_t wo, wn;
-                  if (!rd(o, g, wo) || !rd(nw, g, wn)) return fail("chain read", s, q, v);
+                  if (!rd(o, g, wo) || !rd(nw, g, wn)) return fail("chain read", s, q, i);
                   // lane-wise: the old sample is a summand, so no borrow
                   for (uint32_t sh = 0; sh < 32; sh += 16) {
                     if (((lo[lane] >> sh) & 0xFFFF) < ((prmt4140(wo) >> sh) & 0xFFFF) ||
                         ((hi[lane] >> sh) & 0xFFFF) < ((prmt4342(wo) >> sh) & 0xFFFF))
-                      return fail("chain borrow", s, q, v);
+                      return fail("chain borrow", s, q, i);
                   }
                   lo[lane] = lo[lane] - prmt4140(wo) + prmt4140(wn);
                   hi[lane] = hi[lane] - prmt4342(wo) + prmt4342(wn);
                   partial_ops += 8;
                 }
+                if (dst != 0xFFFFu && store(dst)) return 1;
               }
             }
           }
