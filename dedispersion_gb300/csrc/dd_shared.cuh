@@ -47,26 +47,31 @@ constexpr int kSharedSlots = 3;                         // stages staged at once
 constexpr int kStageRows = kSubMax * kSharedRows;       // rows per stage
 constexpr uint32_t kLaneSeries = 32;                    // series per 16-bit lane (32 * 2040 < 2^16)
 constexpr uint32_t kItemsMax = 32;                      // phase-A items per stage
-// Stage table (u16 units, in shared memory):
+// Stage table (in shared memory; u16 units unless noted):
 //   [0] nsub [1] nrows [2] nitems [3..7] 0
 //   [8 + 4k] bmin_k lo, [+1] bmin_k hi, [+2] first row of k, [+3] program of k
-//   [kTabItems ..)         items: subgroup << 8 | chunk
-//   [kTabSeries ..)        per DM of the tile, kSubMax series offsets (words)
-//   programs, each 8-aligned: [n, ng, nA, nB, dstA, dstB (0xFFFF: no B), 0, 0],
-//   8 row offsets of chain A's first vector, 8 of chain B's, then nA and nB
-//   micro-ops of 4 u16: (old offset, new offset, dst after this one or
-//   0xFFFF, 0)
+//   [kTabItems ..)     items: subgroup << 8 | chunk
+//   [kTabSeries ..)    u32: per DM of the tile, kSubMax series byte offsets
+//                      (from the partial-sum area)
+//   programs (u32, 16-byte aligned): n | ng << 16, nA | nB << 16, dst of
+//   chain A's first vector, dst of chain B's (~0: no chain B), 8 copy-area
+//   byte offsets of A's first vector's rows, 8 of B's, then nA and nB
+//   micro-ops of 4 u32: (old byte offset, new byte offset, dst, 0); dst is
+//   where the series stands after the micro-op (the dummy series when the
+//   vector is not complete yet)
 constexpr uint32_t kTabItems = 8 + 4 * kSubMax;
 constexpr uint32_t kTabSeries = kTabItems + kItemsMax;
+static_assert(kTabSeries % 8 == 0, "series offsets 16-byte aligned");
 
 struct SharedLayout {
   uint32_t raw_bytes;  // bytes staged per row
-  uint32_t off_table, off_raw, off_copy, off_part, zero_word, total;
+  uint32_t off_table, off_raw, off_copy, off_part, zero_word, dummy_word, total;
 };
 
 // Shared memory of one CTA: mbarriers, kSharedSlots stage tables and x
 // kStageRows raw rows, the shifted copies of one stage's rows, `slots`
-// partial-sum series (two copies each) and one zero series.  Host and device
+// partial-sum series (two copies each), one zero series (read for absent
+// subgroups) and one dummy series (written by incomplete vectors).  Host and device
 // use this one formula.
 __host__ __device__ inline SharedLayout make_shared_layout(uint32_t cw, uint32_t psw,
                                                            uint32_t slots,
@@ -80,7 +85,8 @@ __host__ __device__ inline SharedLayout make_shared_layout(uint32_t cw, uint32_t
   L.off_copy = round_up(L.off_raw + kSharedSlots * kStageRows * L.raw_bytes, 128u);
   L.off_part = round_up(L.off_copy + kStageRows * 4u * cw * 4u, 128u);
   L.zero_word = 2u * slots * psw;
-  L.total = L.off_part + (2u * slots + 1u) * psw * 4u;
+  L.dummy_word = L.zero_word + psw;
+  L.total = L.off_part + (2u * slots + 3u) * psw * 4u;
   return L;
 }
 
@@ -128,7 +134,7 @@ __device__ __forceinline__ void shared_copy(const ProblemDesc &P, const uint4 &i
   const uint32_t r = (uint32_t)tid >> 4, c0 = (uint32_t)tid & 15u;
   if ((info.z & kRowPresent) && P.tma) {
     const uint32_t a = align_samples(P.bits);
-    const uint32_t ws = (t0 + (info.z & ~kRowPresent)) / a * a;
+    const uint32_t ws = (t0 + (info.z & ~kRowPresent)) & ~(a - 1u);
     const uint64_t boff = (uint64_t)ws * P.bits / 8u;
     const uint64_t avail = P.row_bytes - boff;
     const uint8_t *src = P.in + (((uint64_t)info.y << 32) | info.x) + boff;
@@ -219,7 +225,7 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
       for (uint32_t r = ty; r < tb[1]; r += TY) {
         const uint4 info = shared_row_info(P, g_index, sbeg + s, r);
         const uint32_t bm = info.z & ~kRowPresent;
-        const uint64_t boff = (uint64_t)((t0 + bm) / a * a) * P.bits / 8u;
+        const uint64_t boff = (uint64_t)((t0 + bm) & ~(a - 1u)) * P.bits / 8u;
         const uint8_t *src = P.in + (((uint64_t)info.y << 32) | info.x);
         uint8_t *dst = rs + r * L.raw_bytes;
         for (uint32_t b = tx; b < L.raw_bytes; b += 32)
@@ -236,7 +242,7 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
       for (uint32_t r = (TY >= kStageRows ? ty % kStageRows : ty); r < nrows; r += kRowStep) {
         const uint32_t k = (r >= tb[8 + 4 + 2]) + (r >= tb[8 + 8 + 2]) + (r >= tb[8 + 12 + 2]);
         const uint32_t bm = tb[8 + 4 * k] | ((uint32_t)tb[8 + 4 * k + 1] << 16);
-        const uint32_t xw = ((t0 + bm) % a) >> 2;
+        const uint32_t xw = ((t0 + bm) & (a - 1u)) >> 2;
         const uint8_t *row = rs + r * L.raw_bytes;
         uint32_t *dst = copy + r * 4u * cw;
         const uint32_t k0 = 2u * (tx + 32u * (TY >= kStageRows ? ty / kStageRows : 0));
@@ -277,23 +283,26 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
     const uint32_t nitems = tb[2];
     for (uint32_t it = ty; it < nitems; it += TY) {
       const uint32_t item = tb[kTabItems + it];
-      const uint16_t *prog = tb + tb[8 + 4 * (item >> 8) + 3];
+      const uint32_t *prog = reinterpret_cast<const uint32_t *>(tb + tb[8 + 4 * (item >> 8) + 3]);
       const uint4 hdr = *reinterpret_cast<const uint4 *>(prog);
       const uint32_t n = hdr.x & 0xFFFFu, ng = hdr.x >> 16;
       const uint32_t nA = hdr.y & 0xFFFFu, nB = hdr.y >> 16;
+      const bool hasB = hdr.w != 0xFFFFFFFFu;
       const uint32_t g = (item & 0xFFu) * 31u + tx;
-      const bool act = g < ng, hasB = (hdr.z >> 16) != 0xFFFFu;
-      const uint32_t gb = copy_s + 4u * g;
+      // Lanes past the series compute its last group again and store nothing.
+      const uint32_t gb = copy_s + 4u * (g < ng ? g : ng - 1u);
+      const bool keep = tx < 31 && g < ng;
+      const uint32_t pg = part_s + 8u * g;
       // lo = (P[4g], P[4g+1]), hi = (P[4g+2], P[4g+3]) as 16-bit lanes.
       uint32_t loA = 0, hiA = 0, loB = 0, hiB = 0;
-      auto rows = [&](const uint16_t *offs, uint32_t &lo, uint32_t &hi) {
-        const uint4 o = *reinterpret_cast<const uint4 *>(offs);
-        const uint32_t off[kSharedRows] = {o.x & 0xFFFFu, o.x >> 16, o.y & 0xFFFFu, o.y >> 16,
-                                           o.z & 0xFFFFu, o.z >> 16, o.w & 0xFFFFu, o.w >> 16};
+      auto rows = [&](const uint32_t *offs, uint32_t &lo, uint32_t &hi) {
+        const uint4 o0 = *reinterpret_cast<const uint4 *>(offs);
+        const uint4 o1 = *reinterpret_cast<const uint4 *>(offs + 4);
+        const uint32_t off[kSharedRows] = {o0.x, o0.y, o0.z, o0.w, o1.x, o1.y, o1.z, o1.w};
 #pragma unroll
         for (int e = 0; e < kSharedRows; ++e) {
           if ((uint32_t)e < n) {
-            const uint32_t w = lds_u32(gb + 4u * off[e]);
+            const uint32_t w = lds_u32(gb + off[e]);
             lo = mad_lo(__byte_perm(w, 0, 0x4140), one, lo);
             hi = mad_lo(__byte_perm(w, 0, 0x4342), one, hi);
           }
@@ -301,46 +310,41 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
       };
       auto store = [&](uint32_t dst, uint32_t lo, uint32_t hi) {
         const uint32_t nlo = __shfl_down_sync(0xffffffffu, lo, 1);
-        if (tx < 31 && act) {
-          const uint32_t pv = part_s + 4u * dst + 8u * g;
-          sts_v2(pv, lo, hi);
-          sts_v2(pv + 4u * psw, __byte_perm(lo, hi, 0x5432), __byte_perm(hi, nlo, 0x5432));
+        if (keep) {
+          sts_v2(pg + dst, lo, hi);
+          sts_v2(pg + dst + 4u * psw, __byte_perm(lo, hi, 0x5432), __byte_perm(hi, nlo, 0x5432));
         }
       };
-      auto step = [&](const uint2 u, uint32_t &lo, uint32_t &hi) {
-        if (act) {
-          const uint32_t wo = lds_u32(gb + 4u * (u.x & 0xFFFFu));
-          const uint32_t wn = lds_u32(gb + 4u * (u.x >> 16));
-          lo = lo - __byte_perm(wo, 0, 0x4140) + __byte_perm(wn, 0, 0x4140);
-          hi = hi - __byte_perm(wo, 0, 0x4342) + __byte_perm(wn, 0, 0x4342);
-        }
+      auto step = [&](const uint4 &u, uint32_t &lo, uint32_t &hi) {
+        const uint32_t wo = lds_u32(gb + u.x);
+        const uint32_t wn = lds_u32(gb + u.y);
+        lo = lo - __byte_perm(wo, 0, 0x4140) + __byte_perm(wn, 0, 0x4140);
+        hi = hi - __byte_perm(wo, 0, 0x4342) + __byte_perm(wn, 0, 0x4342);
       };
-      if (act) {
-        rows(prog + 8, loA, hiA);
-        if (hasB) rows(prog + 16, loB, hiB);
-      }
-      store(hdr.z & 0xFFFFu, loA, hiA);
-      if (hasB) store(hdr.z >> 16, loB, hiB);
-      const uint2 *ua = reinterpret_cast<const uint2 *>(prog + 24);
-      const uint2 *ub = ua + nA;
+      rows(prog + 4, loA, hiA);
+      if (hasB) rows(prog + 12, loB, hiB);
+      store(hdr.z, loA, hiA);
+      if (hasB) store(hdr.w, loB, hiB);
+      const uint4 *ua = reinterpret_cast<const uint4 *>(prog + 20);
+      const uint4 *ub = ua + nA;
       const uint32_t both = nA < nB ? nA : nB;
       uint32_t i = 0;
       for (; i < both; ++i) {
-        const uint2 a = ua[i], b = ub[i];
+        const uint4 a = ua[i], b = ub[i];
         step(a, loA, hiA);
         step(b, loB, hiB);
-        if ((a.y & 0xFFFFu) != 0xFFFFu) store(a.y & 0xFFFFu, loA, hiA);
-        if ((b.y & 0xFFFFu) != 0xFFFFu) store(b.y & 0xFFFFu, loB, hiB);
+        store(a.z, loA, hiA);
+        store(b.z, loB, hiB);
       }
       for (; i < nA; ++i) {
-        const uint2 a = ua[i];
+        const uint4 a = ua[i];
         step(a, loA, hiA);
-        if ((a.y & 0xFFFFu) != 0xFFFFu) store(a.y & 0xFFFFu, loA, hiA);
+        store(a.z, loA, hiA);
       }
       for (; i < nB; ++i) {
-        const uint2 b = ub[i];
+        const uint4 b = ub[i];
         step(b, loB, hiB);
-        if ((b.y & 0xFFFFu) != 0xFFFFu) store(b.y & 0xFFFFu, loB, hiB);
+        store(b.z, loB, hiB);
       }
     }
     __syncthreads();
@@ -351,13 +355,12 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
       since = 0;
     }
     since += kSubMax;
-    const uint16_t *offb = tb + kTabSeries + ty * ND * kSubMax;
+    const uint4 *offb = reinterpret_cast<const uint4 *>(tb + kTabSeries) + ty * ND;
     const uint32_t pb = part_s + 4u * tx;
 #pragma unroll
     for (int j = 0; j < ND; ++j) {
-      const uint2 oo = *reinterpret_cast<const uint2 *>(offb + kSubMax * j);
-      const uint32_t a0 = pb + 4u * (oo.x & 0xFFFFu), a1 = pb + 4u * (oo.x >> 16);
-      const uint32_t a2 = pb + 4u * (oo.y & 0xFFFFu), a3 = pb + 4u * (oo.y >> 16);
+      const uint4 oo = offb[j];
+      const uint32_t a0 = pb + oo.x, a1 = pb + oo.y, a2 = pb + oo.z, a3 = pb + oo.w;
 #pragma unroll
       for (int i = 0; i < NW; ++i) {
         acc[j][i] += lds_u32(a0 + 128u * i) + lds_u32(a1 + 128u * i);

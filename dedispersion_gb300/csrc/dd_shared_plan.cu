@@ -31,6 +31,7 @@ using Vec = std::array<uint8_t, kSharedRows>;
 
 struct Sub {
   uint32_t r0 = 0, n = 0, bmin = 0, spread = 0, maxrel = 0;
+  uint32_t hsum = 0;             // rows moved along the whole chain
   std::vector<Vec> vec;          // chain order
   std::vector<uint32_t> pos;     // per DM of the tile: chain position of its vector
   std::vector<uint32_t> boff;    // per DM: base - bmin
@@ -129,6 +130,7 @@ std::vector<Sub> cut_tile(const std::vector<float> &row_shift, const float *dv, 
         if (h < bh) { bh = h; best = i; }
       }
       cur = left[best];
+      s.hsum += bh;
       left.erase(left.begin() + best);
       chain_pos[cur] = (uint32_t)s.vec.size();
       s.vec.push_back(by_id[cur]);
@@ -185,17 +187,17 @@ std::string build_shared_tables(const KernelInfo &k, const std::vector<float> &r
                  "fewer DMs per tile", spread, DB);
     S.psw = 2 * ng_max;
     S.cw = (maxrel / 4 + ng_max + 2 + 1) & ~1u;
-    if (4ull * kStageRows * S.cw > 65535ull)
-      return fmt("DM spread of %llu samples per tile is too large for 16-bit copy offsets "
-                 "(tile of %llu DMs); use fewer DMs per tile", spread, DB);
-    // Table size bound: header, items, series offsets, and per subgroup a
-    // program of 24 + 4 * (micro-ops <= (nv - 1) * n) entries.
-    const uint32_t prog_max = kSubMax * (24 + 4 * (nv_max - 1) * kSharedRows + 8);
-    const uint32_t tbytes = ((2 * (kTabSeries + kSubMax * DB + prog_max)) + 15) / 16 * 16;
+    // Table size bound: header, items, series offsets, and kSubMax of the
+    // largest program (80 bytes + 16 per micro-op, at most the chain's moved
+    // rows).
+    uint32_t prog_max = 0;
+    for (uint32_t t = 0; t < tiles_d; t++)
+      for (const Sub &s : tiles[t]) prog_max = std::max(prog_max, 80 + 16 * s.hsum);
+    const uint32_t tbytes = 2 * kTabSeries + 16 * DB + kSubMax * (prog_max + 16);
     S.slots = 0;
     for (uint32_t sl = kSubMax * nv_cap; sl >= 1; sl--) {
       const SharedLayout L = make_shared_layout(S.cw, S.psw, sl, tbytes, bits);
-      if (L.total <= smem_budget && (2ull * sl + 1) * S.psw <= 65536ull) {
+      if (L.total <= smem_budget) {
         S.slots = sl;
         S.table_bytes = tbytes;
         S.smem = L.total;
@@ -208,7 +210,8 @@ std::string build_shared_tables(const KernelInfo &k, const std::vector<float> &r
     if (S.slots >= nv_max) break;
     nv_cap = S.slots;  // fewer rows per subgroup, so that one always fits
   }
-  const uint32_t zero_word = 2 * S.slots * S.psw;
+  const SharedLayout L0 = make_shared_layout(S.cw, S.psw, S.slots, S.table_bytes, bits);
+  const uint32_t zero_bytes = 4 * L0.zero_word, dummy_bytes = 4 * L0.dummy_word;
 
   S.tile_stage.push_back(0);
   uint32_t tb_max = 16;
@@ -233,7 +236,15 @@ std::string build_shared_tables(const KernelInfo &k, const std::vector<float> &r
       const uint32_t nsub = (uint32_t)(end - i);
       while (S.pool.size() % 8) S.pool.push_back(0);
       const size_t at = S.pool.size();
-      std::vector<uint16_t> tb(kTabSeries + kSubMax * DB, 0);
+      std::vector<uint16_t> tb(kTabSeries + 2 * kSubMax * DB, 0);
+      auto put32 = [&](size_t u16_index, uint32_t v) {
+        tb[u16_index] = (uint16_t)(v & 0xFFFFu);
+        tb[u16_index + 1] = (uint16_t)(v >> 16);
+      };
+      auto push32 = [&](uint32_t v) {
+        tb.push_back((uint16_t)(v & 0xFFFFu));
+        tb.push_back((uint16_t)(v >> 16));
+      };
       tb[0] = (uint16_t)nsub;
       tb[1] = (uint16_t)rows;
       SharedStage st{};
@@ -242,10 +253,10 @@ std::string build_shared_tables(const KernelInfo &k, const std::vector<float> &r
       st.nrows = (uint16_t)rows;
       st.nsub = (uint16_t)nsub;
       uint32_t rstart = 0, slot = 0, nitems = 0;
-      std::vector<uint32_t> slot0(kSubMax, 0);
       for (uint32_t q = 0; q < (uint32_t)kSubMax; q++) {
         if (q >= nsub) {
           tb[8 + 4 * q + 2] = 0xFFFF;
+          for (uint32_t j = 0; j < DB; j++) put32(kTabSeries + 2 * (j * kSubMax + q), zero_bytes);
           continue;
         }
         const Sub &s = subs[i + q];
@@ -257,18 +268,17 @@ std::string build_shared_tables(const KernelInfo &k, const std::vector<float> &r
         for (uint32_t e = 0; e < s.n; e++) st.row_sub[rstart + e] = (uint8_t)q;
         for (uint32_t c = 0; c < ceil_div(ng, 31); c++)
           tb[kTabItems + nitems++] = (uint16_t)(q << 8 | c);
-        slot0[q] = slot;
-        // series offsets of every DM
+        // series byte offsets of every DM: copy (base & 1), word (base >> 1)
         for (uint32_t j = 0; j < DB; j++) {
           const uint32_t b = s.boff[j];
-          tb[kTabSeries + j * kSubMax + q] =
-              (uint16_t)((2 * (slot + s.pos[j]) + (b & 1u)) * S.psw + (b >> 1));
+          put32(kTabSeries + 2 * (j * kSubMax + q),
+                4 * ((2 * (slot + s.pos[j]) + (b & 1u)) * S.psw + (b >> 1)));
         }
         // program
         while (tb.size() % 8) tb.push_back(0);
         tb[8 + 4 * q + 3] = (uint16_t)tb.size();
         auto off = [&](uint32_t e, uint32_t rel) {
-          return (uint16_t)((rstart + e) * 4 * S.cw + (rel & 3u) * S.cw + (rel >> 2));
+          return 4 * ((rstart + e) * 4 * S.cw + (rel & 3u) * S.cw + (rel >> 2));
         };
         const uint32_t nvq = (uint32_t)s.vec.size();
         std::vector<uint32_t> h(nvq, 0);  // rows moved from vector v - 1 to v
@@ -287,47 +297,41 @@ std::string build_shared_tables(const KernelInfo &k, const std::vector<float> &r
           }
         }
         const bool hasB = m < nvq;
-        auto dst_of = [&](uint32_t v) { return (uint16_t)(2 * (slot + v) * S.psw); };
-        std::vector<uint16_t> ua, ub;
-        auto uops = [&](std::vector<uint16_t> &u, uint32_t from, uint32_t to) {
+        auto dst_of = [&](uint32_t v) { return 4 * 2 * (slot + v) * S.psw; };
+        std::vector<uint32_t> ua, ub;
+        auto uops = [&](std::vector<uint32_t> &u, uint32_t from, uint32_t to) {
           for (uint32_t v = from + 1; v < to; v++) {
             uint32_t left = h[v];
             for (uint32_t e = 0; e < s.n; e++)
               if (s.vec[v - 1][e] != s.vec[v][e]) {
                 u.push_back(off(e, s.vec[v - 1][e]));
                 u.push_back(off(e, s.vec[v][e]));
-                u.push_back(--left == 0 ? dst_of(v) : (uint16_t)0xFFFF);
+                u.push_back(--left == 0 ? dst_of(v) : dummy_bytes);
                 u.push_back(0);
               }
           }
         };
         uops(ua, 0, m);
         if (hasB) uops(ub, m, nvq);
-        tb.push_back((uint16_t)s.n);
-        tb.push_back((uint16_t)ng);
-        tb.push_back((uint16_t)(ua.size() / 4));
-        tb.push_back((uint16_t)(ub.size() / 4));
-        tb.push_back(dst_of(0));
-        tb.push_back(hasB ? dst_of(m) : (uint16_t)0xFFFF);
-        tb.push_back(0);
-        tb.push_back(0);
+        push32(s.n | ng << 16);
+        push32((uint32_t)(ua.size() / 4) | (uint32_t)(ub.size() / 4) << 16);
+        push32(dst_of(0));
+        push32(hasB ? dst_of(m) : 0xFFFFFFFFu);
+        for (uint32_t e = 0; e < (uint32_t)kSharedRows; e++) push32(e < s.n ? off(e, s.vec[0][e]) : 0);
         for (uint32_t e = 0; e < (uint32_t)kSharedRows; e++)
-          tb.push_back(e < s.n ? off(e, s.vec[0][e]) : (uint16_t)0);
-        for (uint32_t e = 0; e < (uint32_t)kSharedRows; e++)
-          tb.push_back(hasB && e < s.n ? off(e, s.vec[m][e]) : (uint16_t)0);
-        tb.insert(tb.end(), ua.begin(), ua.end());
-        tb.insert(tb.end(), ub.begin(), ub.end());
+          push32(hasB && e < s.n ? off(e, s.vec[m][e]) : 0);
+        for (uint32_t w : ua) push32(w);
+        for (uint32_t w : ub) push32(w);
         const uint64_t row_ops = s.n * (hasB ? 2u : 1u) + 2 * (ua.size() + ub.size()) / 4;
         S.adds_partial += row_ops * 4 * ng;
         S.adds_series += (uint64_t)DB * T;
         slot += nvq;
         rstart += s.n;
       }
-      for (uint32_t q = nsub; q < (uint32_t)kSubMax; q++)
-        for (uint32_t j = 0; j < DB; j++) tb[kTabSeries + j * kSubMax + q] = (uint16_t)zero_word;
       tb[2] = (uint16_t)nitems;
       while (tb.size() % 8) tb.push_back(0);
       st.nitems = (uint16_t)nitems;
+      if (tb.size() * 2 > 65535) return fmt("stage table of %llu bytes (limit %llu)", tb.size() * 2, 65535);
       st.table_bytes = (uint16_t)(tb.size() * 2);
       tb_max = std::max<uint32_t>(tb_max, st.table_bytes);
       S.pool.insert(S.pool.end(), tb.begin(), tb.end());

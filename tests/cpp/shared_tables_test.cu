@@ -80,7 +80,8 @@ int main(int argc, char **argv) {
     return in[(size_t)r * rowlen + pos];
   };
   uint64_t checked = 0, stages = 0, partial_ops = 0;
-  std::vector<uint32_t> copy(kStageRows * 4 * cw), part((2 * tab.slots + 1) * psw, 0);
+  std::vector<uint32_t> copy(kStageRows * 4 * cw), part((2 * tab.slots + 3) * psw, 0);
+  const size_t dummy0 = (size_t)L.dummy_word, dummy1 = dummy0 + 2 * psw;
   std::vector<uint8_t> written(part.size());
   for (uint32_t dt = 0; dt < tiles_d; dt++) {
     for (uint32_t tt = 0; tt < std::min(ntt, tiles_t); tt++) {
@@ -99,6 +100,7 @@ int main(int argc, char **argv) {
           if (i >= tlen) throw i;
           return tb[i];
         };
+        auto T32 = [&](size_t i) -> uint32_t { return T16(i) | (T16(i + 1) << 16); };
         try {
           const uint32_t nsub = T16(0), nrows = T16(1), nitems = T16(2);
           if (nsub != st.nsub || nrows != st.nrows || nitems != st.nitems || nsub < 1 ||
@@ -124,8 +126,10 @@ int main(int argc, char **argv) {
           }
           // phase A
           std::fill(written.begin(), written.end(), 0);
-          for (size_t w = 2 * tab.slots * psw; w < part.size(); w++) written[w] = 1;  // zero series
-          auto rd = [&](uint32_t off, uint32_t g, uint32_t &w) {
+          for (size_t w = 2 * tab.slots * psw; w < dummy0; w++) written[w] = 1;  // zero series
+          auto rd = [&](uint32_t offb, uint32_t g, uint32_t &w) {
+            if (offb % 4) return false;
+            const uint32_t off = offb / 4;
             if ((size_t)off + g >= copy.size()) return false;
             if ((off % cw) + g >= cw) return false;  // stays in its copy of its row
             if (off / (4 * cw) >= nrows) return false;
@@ -137,42 +141,47 @@ int main(int argc, char **argv) {
             if (q >= nsub) return fail("item subgroup", s, it, q);
             const uint32_t pg = T16(8 + 4 * q + 3);
             if (pg % 8) return fail("program alignment", s, q, pg);
-            const uint32_t n = T16(pg), ng = T16(pg + 1), nA = T16(pg + 2), nB = T16(pg + 3);
-            const uint32_t dA = T16(pg + 4), dB = T16(pg + 5);
+            const uint32_t n = T32(pg) & 0xFFFF, ng = T32(pg) >> 16;
+            const uint32_t nA = T32(pg + 2) & 0xFFFF, nB = T32(pg + 2) >> 16;
+            const uint32_t dA = T32(pg + 4), dB = T32(pg + 6);
             if (n < 1 || n > (uint32_t)kSharedRows) return fail("program rows", s, q, n);
             // both half-chains of every lane of the chunk
             for (uint32_t half = 0; half < 2; half++) {
               const uint32_t d0 = half ? dB : dA;
-              if (half && d0 == 0xFFFFu) {
+              if (half && d0 == 0xFFFFFFFFu) {
                 if (nB) return fail("half B without start", s, q, nB);
                 break;
               }
               uint32_t lo[32] = {0}, hi[32] = {0};
               for (uint32_t lane = 0; lane < 32; lane++) {
-                const uint32_t g = c * 31 + lane;
-                if (g >= ng) continue;
+                const uint32_t g = std::min(c * 31 + lane, ng - 1);  // lanes past the series
                 for (uint32_t e = 0; e < n; e++) {
                   uint32_t w;
-                  if (!rd(T16(pg + 8 + 8 * half + e), g, w)) return fail("copy read", s, q, e);
+                  if (!rd(T32(pg + 8 + 16 * half + 2 * e), g, w)) return fail("copy read", s, q, e);
                   lo[lane] += prmt4140(w);
                   hi[lane] += prmt4342(w);
                 }
-                partial_ops += 4 * n;
+                if (c * 31 + lane < ng) partial_ops += 4 * n;
               }
-              auto store = [&](uint32_t dst) {
+              auto store = [&](uint32_t dstb) {
+                if (dstb % 4) return fail("dst alignment", s, q, dstb);
+                const size_t dst = dstb / 4;
+                const bool dummy = dst == dummy0;
                 for (uint32_t lane = 0; lane < 31; lane++) {
                   const uint32_t g = c * 31 + lane;
                   if (g >= ng) continue;
                   const uint32_t nlo = lo[lane + 1];
-                  const size_t c0 = (size_t)dst + 2 * g, c1 = c0 + psw;
-                  if (dst % (2 * psw) || 2 * g + 1 >= psw || c1 + 1 >= 2 * (size_t)tab.slots * psw)
-                    return fail("series write", s, dst, g);
+                  const size_t c0 = dst + 2 * g, c1 = c0 + psw;
+                  if (!dummy && (dst % (2 * psw) || c1 + 1 >= 2 * (size_t)tab.slots * psw))
+                    return fail("series write", s, (long)dst, g);
+                  if (2 * g + 1 >= psw || (dummy && c1 + 1 >= dummy1)) return fail("series length", s, (long)dst, g);
+                  if (dummy) continue;
                   part[c0] = lo[lane];
                   part[c0 + 1] = hi[lane];
                   part[c1] = (lo[lane] >> 16) | (hi[lane] << 16);
                   part[c1 + 1] = (hi[lane] >> 16) | (nlo << 16);
                   written[c0] = written[c0 + 1] = written[c1] = 1;
-                  written[c1 + 1] = g + 1 < ng ? 1 : 2;  // 2: holds a zero neighbour
+                  written[c1 + 1] = g + 1 < ng ? 1 : 2;  // 2: neighbour past the series
                   for (uint32_t x : {lo[lane], hi[lane]})
                     if ((x & 0xFFFF) > 8 * 255 || (x >> 16) > 8 * 255)
                       return fail("lane range", s, g, x);
@@ -180,14 +189,13 @@ int main(int argc, char **argv) {
                 return 0;
               };
               if (store(d0)) return 1;
-              const size_t u0 = pg + 24 + (half ? 4 * nA : 0);
+              const size_t u0 = pg + 40 + 8 * (half ? nA : 0);
               const uint32_t nu = half ? nB : nA;
               for (uint32_t i = 0; i < nu; i++) {
-                const uint32_t o = T16(u0 + 4 * i), nw = T16(u0 + 4 * i + 1);
-                const uint32_t dst = T16(u0 + 4 * i + 2);
+                const uint32_t o = T32(u0 + 8 * i), nw = T32(u0 + 8 * i + 2);
+                const uint32_t dst = T32(u0 + 8 * i + 4);
                 for (uint32_t lane = 0; lane < 32; lane++) {
-                  const uint32_t g = c * 31 + lane;
-                  if (g >= ng) continue;
+                  const uint32_t g = std::min(c * 31 + lane, ng - 1);
                   uint32_t wo, wn;
                   if (!rd(o, g, wo) || !rd(nw, g, wn)) return fail("chain read", s, q, i);
                   // lane-wise: the old sample is a summand, so no borrow
@@ -198,9 +206,9 @@ int main(int argc, char **argv) {
                   }
                   lo[lane] = lo[lane] - prmt4140(wo) + prmt4140(wn);
                   hi[lane] = hi[lane] - prmt4342(wo) + prmt4342(wn);
-                  partial_ops += 8;
+                  if (c * 31 + lane < ng) partial_ops += 8;
                 }
-                if (dst != 0xFFFFu && store(dst)) return 1;
+                if (store(dst)) return 1;
               }
             }
           }
@@ -216,10 +224,12 @@ int main(int argc, char **argv) {
           since += kSubMax;
           for (uint32_t j = 0; j < DB; j++)
             for (uint32_t q = 0; q < (uint32_t)kSubMax; q++) {
-              const uint32_t off = T16(kTabSeries + j * kSubMax + q);
+              const uint32_t offb = T32(kTabSeries + 2 * (j * kSubMax + q));
+              if (offb % 4) return fail("series offset alignment", s, j, q);
+              const uint32_t off = offb / 4;
               for (uint32_t i = 0; i < T / 2; i++) {
                 const size_t w = (size_t)off + i;
-                if (w >= part.size()) return fail("series read", s, j, i);
+                if (w >= dummy0) return fail("series read", s, j, i);
                 if (written[w] != 1) return fail("unwritten series word", s, j, (long)w);
                 const uint32_t a = acc[(size_t)j * (T / 2) + i] + part[w];
                 if ((a & 0xFFFF) < (acc[(size_t)j * (T / 2) + i] & 0xFFFF) && (part[w] & 0xFFFF))
