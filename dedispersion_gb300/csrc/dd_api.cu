@@ -190,6 +190,22 @@ const dd::KernelInfo *find_kernel(dd_mode mode, uint32_t bits, const dd_conf &c)
   return nullptr;
 }
 
+// The default configuration of a mode and input width: the first registry
+// entry of its family; for single-step input of 1-8 bits the first
+// shared-partial-sum entry when `shared` (plans fall back to the direct
+// entry where a shape does not fit the shared tables).
+const dd::KernelInfo *default_kernel(dd_mode mode, uint32_t bits, bool shared) {
+  int n = 0;
+  const dd::KernelInfo *reg = dd::kernel_registry(&n);
+  const uint32_t fb = family_bits(mode, bits);
+  const bool want_shared = shared && mode == DD_SINGLE_STEP && bits <= 8;
+  for (int i = 0; i < n; i++)
+    if ((uint32_t)reg[i].elem_bits == fb &&
+        (reg[i].family == dd::kFamilyShared8) == want_shared)
+      return &reg[i];
+  return nullptr;
+}
+
 dd_conf conf_of(const dd::KernelInfo &k) {
   dd_conf c{};
   c.split_batches = 0; c.local_mem = 1; c.unroll = k.channels;
@@ -259,6 +275,9 @@ struct dd_plan {
   size_t cap_stage_rows = 0, cap_tile_stage = 0, cap_pool = 0;
   std::string invalid;  // why the tables are not usable (empty when ready)
   bool ready = false;
+  // Created without a configuration: a shape that the default shared kernel
+  // cannot take runs on the default direct kernel instead.
+  bool auto_kernel = false;
 };
 
 namespace {
@@ -508,6 +527,18 @@ dd_status rebuild(dd_plan *p) {
   return DD_OK;
 }
 
+// rebuild(), and for plans created without a configuration: the default
+// shared kernel, else (a shape it cannot take) the default direct kernel.
+dd_status rebuild_auto(dd_plan *p) {
+  if (p->auto_kernel) p->kinfo = default_kernel(p->mode, p->bits, true);
+  dd_status st = rebuild(p);
+  if (st == DD_ERR_UNSUPPORTED && p->auto_kernel && p->kinfo->family == dd::kFamilyShared8) {
+    p->kinfo = default_kernel(p->mode, p->bits, false);
+    st = rebuild(p);
+  }
+  return st;
+}
+
 }  // namespace
 
 namespace dd {
@@ -663,15 +694,10 @@ dd_status dd_default_conf(const dd_observation *o, dd_mode mode, uint32_t input_
   if (!conf) return fail(DD_ERR_INVALID_ARGUMENT, "conf is NULL");
   if (mode == DD_STEP_TWO) input_bits = 32;
   if (!bits_ok(input_bits)) return fail(DD_ERR_UNSUPPORTED, "input_bits %u not supported", input_bits);
-  int n = 0;
-  const dd::KernelInfo *reg = dd::kernel_registry(&n);
-  const uint32_t fb = family_bits(mode, input_bits);
-  for (int i = 0; i < n; i++)
-    if ((uint32_t)reg[i].elem_bits == fb) {
-      *conf = conf_of(reg[i]);
-      return DD_OK;
-    }
-  return fail(DD_ERR_UNSUPPORTED, "no kernel for %u-bit input", input_bits);
+  const dd::KernelInfo *k = default_kernel(mode, input_bits, true);
+  if (!k) return fail(DD_ERR_UNSUPPORTED, "no kernel for %u-bit input", input_bits);
+  *conf = conf_of(*k);
+  return DD_OK;
 }
 
 dd_status dd_conf_print(const dd_conf *c, char *text, size_t capacity) {
@@ -756,6 +782,7 @@ dd_status dd_plan_create(dd_plan **plan, const dd_observation *o, dd_mode mode,
   dd_plan *p = new dd_plan();
   p->device = device; p->obs = *o; p->mode = mode; p->bits = input_bits; p->padding = padding;
   p->kinfo = k;
+  p->auto_kernel = conf == nullptr;
   p->dims = dims_of(o, mode, input_bits, padding);
   {
     DeviceGuard g(device);
@@ -814,7 +841,7 @@ namespace {
 // inconsistent in between (delays checked before the zapped mask arrives):
 // such errors are kept and reported by the next run; device errors return.
 dd_status rebuild_deferred(dd_plan *p) {
-  dd_status st = rebuild(p);
+  dd_status st = rebuild_auto(p);
   if (st == DD_ERR_INVALID_ARGUMENT || st == DD_ERR_UNSUPPORTED) {
     p->invalid = g_error;
     return DD_OK;
@@ -1034,7 +1061,7 @@ dd_status run_sync(const dd_observation *o, dd_mode mode, const uint32_t *zapped
     }
   }
   if (dirty) {
-    st = rebuild(c.plan);
+    st = rebuild_auto(c.plan);
     if (st) {
       c.shifts.clear();
       return st;

@@ -246,7 +246,11 @@ dd_status dd_batch_commit(dd_batch *b) {
   DDB_CUDA(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device),
            "query shared memory");
   DDB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device), "query SMs");
-  const size_t static_smem = sizeof(dd::ProblemDesc) + 64;
+  // The kernel's own static shared memory (the problem descriptor) comes out
+  // of the same per-block budget.
+  cudaFuncAttributes fa{};
+  DDB_CUDA(cudaFuncGetAttributes(&fa, batch_kernel), "query kernel attributes");
+  const size_t static_smem = fa.sharedSizeBytes;
   if (L.total + static_smem > (size_t)smem_max)
     return fail(DD_ERR_UNSUPPORTED, "batch window needs %u bytes of shared memory", L.total);
   DDB_CUDA(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,

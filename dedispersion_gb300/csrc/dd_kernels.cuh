@@ -43,9 +43,11 @@ __global__ void __launch_bounds__(32 * TY, (TY >= 16 ? 1 : 2))
     for (int r = 0; r < kSharedSlots; ++r) mbar_init(bars + r, blockDim.x);
     fence_mbar_init();
   }
-  // The zero series that absent subgroups of a stage read.
+  // The zero series that absent subgroups of a stage read, and the zero row.
   uint32_t *zero = reinterpret_cast<uint32_t *>(smem + L.off_part) + L.zero_word;
   for (uint32_t w = threadIdx.x; w < P.psw; w += blockDim.x) zero[w] = 0;
+  uint32_t *zrow = reinterpret_cast<uint32_t *>(smem + L.off_copy) + L.zero_copy;
+  for (uint32_t w = threadIdx.x; w < P.cw; w += blockDim.x) zrow[w] = 0;
   __syncthreads();
   uint32_t g, dtile, ttile, sc = 0;
   decode_tile(P, blockIdx.x, g, dtile, ttile);

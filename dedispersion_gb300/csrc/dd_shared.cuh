@@ -58,18 +58,19 @@ constexpr uint32_t kItemsMax = 32;                      // phase-A items per sta
 //   byte offsets of A's first vector's rows, 8 of B's, then nA and nB
 //   micro-ops of 4 u32: (old byte offset, new byte offset, dst, 0); dst is
 //   where the series stands after the micro-op (the dummy series when the
-//   vector is not complete yet)
+//   vector is not complete yet); nA == nB whenever chain B exists
 constexpr uint32_t kTabItems = 8 + 4 * kSubMax;
 constexpr uint32_t kTabSeries = kTabItems + kItemsMax;
 static_assert(kTabSeries % 8 == 0, "series offsets 16-byte aligned");
 
 struct SharedLayout {
   uint32_t raw_bytes;  // bytes staged per row
-  uint32_t off_table, off_raw, off_copy, off_part, zero_word, dummy_word, total;
+  uint32_t off_table, off_raw, off_copy, zero_copy, off_part, zero_word, dummy_word, total;
 };
 
 // Shared memory of one CTA: mbarriers, kSharedSlots stage tables and x
-// kStageRows raw rows, the shifted copies of one stage's rows, `slots`
+// kStageRows raw rows, the shifted copies of one stage's rows (and one zero
+// row, which rows past a subgroup's end and no-op micro-ops read), `slots`
 // partial-sum series (two copies each), one zero series (read for absent
 // subgroups) and one dummy series (written by incomplete vectors).  Host and device
 // use this one formula.
@@ -83,7 +84,8 @@ __host__ __device__ inline SharedLayout make_shared_layout(uint32_t cw, uint32_t
   L.off_table = 128;
   L.off_raw = round_up(L.off_table + kSharedSlots * table_bytes, 128u);
   L.off_copy = round_up(L.off_raw + kSharedSlots * kStageRows * L.raw_bytes, 128u);
-  L.off_part = round_up(L.off_copy + kStageRows * 4u * cw * 4u, 128u);
+  L.zero_copy = kStageRows * 4u * cw;  // cw zero words after the copies
+  L.off_part = round_up(L.off_copy + (kStageRows * 4u + 1u) * cw * 4u, 128u);
   L.zero_word = 2u * slots * psw;
   L.dummy_word = L.zero_word + psw;
   L.total = L.off_part + (2u * slots + 3u) * psw * 4u;
@@ -286,13 +288,15 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
       const uint32_t *prog = reinterpret_cast<const uint32_t *>(tb + tb[8 + 4 * (item >> 8) + 3]);
       const uint4 hdr = *reinterpret_cast<const uint4 *>(prog);
       const uint32_t n = hdr.x & 0xFFFFu, ng = hdr.x >> 16;
-      const uint32_t nA = hdr.y & 0xFFFFu, nB = hdr.y >> 16;
+      const uint32_t nA = hdr.y & 0xFFFFu;
       const bool hasB = hdr.w != 0xFFFFFFFFu;
       const uint32_t g = (item & 0xFFu) * 31u + tx;
       // Lanes past the series compute its last group again and store nothing.
       const uint32_t gb = copy_s + 4u * (g < ng ? g : ng - 1u);
+      // Stores of lanes that keep nothing go to the dummy series.
       const bool keep = tx < 31 && g < ng;
       const uint32_t pg = part_s + 8u * g;
+      const uint32_t junk = part_s + 4u * L.dummy_word + 8u * tx;
       // lo = (P[4g], P[4g+1]), hi = (P[4g+2], P[4g+3]) as 16-bit lanes.
       uint32_t loA = 0, hiA = 0, loB = 0, hiB = 0;
       auto rows = [&](const uint32_t *offs, uint32_t &lo, uint32_t &hi) {
@@ -300,20 +304,17 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
         const uint4 o1 = *reinterpret_cast<const uint4 *>(offs + 4);
         const uint32_t off[kSharedRows] = {o0.x, o0.y, o0.z, o0.w, o1.x, o1.y, o1.z, o1.w};
 #pragma unroll
-        for (int e = 0; e < kSharedRows; ++e) {
-          if ((uint32_t)e < n) {
-            const uint32_t w = lds_u32(gb + off[e]);
-            lo = mad_lo(__byte_perm(w, 0, 0x4140), one, lo);
-            hi = mad_lo(__byte_perm(w, 0, 0x4342), one, hi);
-          }
+        for (int e = 0; e < kSharedRows; ++e) {  // rows past n read the zero row
+          const uint32_t w = lds_u32(gb + off[e]);
+          lo = mad_lo(__byte_perm(w, 0, 0x4140), one, lo);
+          hi = mad_lo(__byte_perm(w, 0, 0x4342), one, hi);
         }
       };
       auto store = [&](uint32_t dst, uint32_t lo, uint32_t hi) {
         const uint32_t nlo = __shfl_down_sync(0xffffffffu, lo, 1);
-        if (keep) {
-          sts_v2(pg + dst, lo, hi);
-          sts_v2(pg + dst + 4u * psw, __byte_perm(lo, hi, 0x5432), __byte_perm(hi, nlo, 0x5432));
-        }
+        const uint32_t at = keep ? pg + dst : junk;
+        sts_v2(at, lo, hi);
+        sts_v2(at + 4u * psw, __byte_perm(lo, hi, 0x5432), __byte_perm(hi, nlo, 0x5432));
       };
       auto step = [&](const uint4 &u, uint32_t &lo, uint32_t &hi) {
         const uint32_t wo = lds_u32(gb + u.x);
@@ -325,25 +326,15 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
       if (hasB) rows(prog + 12, loB, hiB);
       store(hdr.z, loA, hiA);
       if (hasB) store(hdr.w, loB, hiB);
+      // Chain B exists whenever there are micro-ops; the host pads the two
+      // halves to the same length with no-op micro-ops.
       const uint4 *ua = reinterpret_cast<const uint4 *>(prog + 20);
       const uint4 *ub = ua + nA;
-      const uint32_t both = nA < nB ? nA : nB;
-      uint32_t i = 0;
-      for (; i < both; ++i) {
+      for (uint32_t i = 0; i < nA; ++i) {
         const uint4 a = ua[i], b = ub[i];
         step(a, loA, hiA);
         step(b, loB, hiB);
         store(a.z, loA, hiA);
-        store(b.z, loB, hiB);
-      }
-      for (; i < nA; ++i) {
-        const uint4 a = ua[i];
-        step(a, loA, hiA);
-        store(a.z, loA, hiA);
-      }
-      for (; i < nB; ++i) {
-        const uint4 b = ub[i];
-        step(b, loB, hiB);
         store(b.z, loB, hiB);
       }
     }

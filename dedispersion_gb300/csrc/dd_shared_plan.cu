@@ -185,8 +185,8 @@ std::string build_shared_tables(const KernelInfo &k, const std::vector<float> &r
     if (ceil_div(ng_max, 31) > kItemsMax)
       return fmt("DM spread of %llu samples per tile is too large (tile of %llu DMs); use "
                  "fewer DMs per tile", spread, DB);
-    S.psw = 2 * ng_max;
-    S.cw = (maxrel / 4 + ng_max + 2 + 1) & ~1u;
+    S.psw = std::max<uint32_t>(2 * ng_max, 64);  // the dummy series takes 32 lanes' junk stores
+    S.cw = std::max<uint32_t>((maxrel / 4 + ng_max + 2 + 1) & ~1u, ng_max);  // zero row >= ng
     // Table size bound: header, items, series offsets, and kSubMax of the
     // largest program (80 bytes + 16 per micro-op, at most the chain's moved
     // rows).
@@ -212,6 +212,7 @@ std::string build_shared_tables(const KernelInfo &k, const std::vector<float> &r
   }
   const SharedLayout L0 = make_shared_layout(S.cw, S.psw, S.slots, S.table_bytes, bits);
   const uint32_t zero_bytes = 4 * L0.zero_word, dummy_bytes = 4 * L0.dummy_word;
+  const uint32_t zero_row = 4 * L0.zero_copy;  // copy-area byte offset of the zero row
 
   S.tile_stage.push_back(0);
   uint32_t tb_max = 16;
@@ -313,16 +314,21 @@ std::string build_shared_tables(const KernelInfo &k, const std::vector<float> &r
         };
         uops(ua, 0, m);
         if (hasB) uops(ub, m, nvq);
+        // Pad the shorter half with no-op micro-ops (zero row in and out,
+        // result to the dummy series): the kernel steps both in lockstep.
+        while (hasB && ua.size() < ub.size()) ua.insert(ua.end(), {zero_row, zero_row, dummy_bytes, 0});
+        while (hasB && ub.size() < ua.size()) ub.insert(ub.end(), {zero_row, zero_row, dummy_bytes, 0});
         push32(s.n | ng << 16);
         push32((uint32_t)(ua.size() / 4) | (uint32_t)(ub.size() / 4) << 16);
         push32(dst_of(0));
         push32(hasB ? dst_of(m) : 0xFFFFFFFFu);
-        for (uint32_t e = 0; e < (uint32_t)kSharedRows; e++) push32(e < s.n ? off(e, s.vec[0][e]) : 0);
         for (uint32_t e = 0; e < (uint32_t)kSharedRows; e++)
-          push32(hasB && e < s.n ? off(e, s.vec[m][e]) : 0);
+          push32(e < s.n ? off(e, s.vec[0][e]) : zero_row);
+        for (uint32_t e = 0; e < (uint32_t)kSharedRows; e++)
+          push32(hasB && e < s.n ? off(e, s.vec[m][e]) : zero_row);
         for (uint32_t w : ua) push32(w);
         for (uint32_t w : ub) push32(w);
-        const uint64_t row_ops = s.n * (hasB ? 2u : 1u) + 2 * (ua.size() + ub.size()) / 4;
+        const uint64_t row_ops = kSharedRows * (hasB ? 2u : 1u) + 2 * (ua.size() + ub.size()) / 4;
         S.adds_partial += row_ops * 4 * ng;
         S.adds_series += (uint64_t)DB * T;
         slot += nvq;

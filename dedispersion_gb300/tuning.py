@@ -48,8 +48,11 @@ class TuneResult:
 
 
 def family_kernels(mode: int, bits: int):
+    """Compiled configurations for a mode and input width; the
+    shared-partial-sum ones (items_d2 = 8) compute single-step input only."""
     fam = 32 if mode == DD_STEP_TWO else (8 if bits <= 8 else bits)
-    return [k for k in kernels() if k.elem_bits == fam]
+    return [k for k in kernels() if k.elem_bits == fam and
+            (mode == DD_SINGLE_STEP or k.conf.getNrItemsD2() != 8)]
 
 
 def _time_plan(plan: Plan, d_in, d_out, warmup: int, iterations: int):
@@ -91,7 +94,12 @@ def sweep(obs, mode: int, bits: int, padding: int, shifts, zapped=None, mapping=
     from ._abi import DD_ERR_INVALID_ARGUMENT, DD_ERR_UNSUPPORTED
     for k in (candidates if candidates is not None else family_kernels(mode, bits)):
         t0 = time.perf_counter()
-        plan = Plan(obs, mode, bits, padding, device=device, kernel=k.index)
+        try:
+            plan = Plan(obs, mode, bits, padding, device=device, kernel=k.index)
+        except DedispersionError as e:
+            if e.status == DD_ERR_UNSUPPORTED:
+                continue
+            raise
         try:
             plan.setShifts(shifts)
             if mode != DD_STEP_TWO and zapped is not None:

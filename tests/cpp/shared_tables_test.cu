@@ -80,7 +80,8 @@ int main(int argc, char **argv) {
     return in[(size_t)r * rowlen + pos];
   };
   uint64_t checked = 0, stages = 0, partial_ops = 0;
-  std::vector<uint32_t> copy(kStageRows * 4 * cw), part((2 * tab.slots + 3) * psw, 0);
+  std::vector<uint32_t> copy((kStageRows * 4 + 1) * cw), part((2 * tab.slots + 3) * psw, 0);
+  const size_t zrow = L.zero_copy;
   const size_t dummy0 = (size_t)L.dummy_word, dummy1 = dummy0 + 2 * psw;
   std::vector<uint8_t> written(part.size());
   for (uint32_t dt = 0; dt < tiles_d; dt++) {
@@ -108,6 +109,7 @@ int main(int argc, char **argv) {
             return fail("header", s, nsub, nrows);
           // expansion
           std::fill(copy.begin(), copy.end(), 0xA5A5A5A5u);
+          std::fill(copy.begin() + zrow, copy.end(), 0u);
           for (uint32_t r = 0; r < nrows; r++) {
             const uint32_t q = (r >= T16(8 + 4 + 2)) + (r >= T16(8 + 8 + 2)) + (r >= T16(8 + 12 + 2));
             if (q != st.row_sub[r]) return fail("row subgroup", s, r, q);
@@ -130,6 +132,11 @@ int main(int argc, char **argv) {
           auto rd = [&](uint32_t offb, uint32_t g, uint32_t &w) {
             if (offb % 4) return false;
             const uint32_t off = offb / 4;
+            if (off == zrow) {  // the zero row
+              if (g >= cw) return false;
+              w = 0;
+              return true;
+            }
             if ((size_t)off + g >= copy.size()) return false;
             if ((off % cw) + g >= cw) return false;  // stays in its copy of its row
             if (off / (4 * cw) >= nrows) return false;
@@ -145,6 +152,8 @@ int main(int argc, char **argv) {
             const uint32_t nA = T32(pg + 2) & 0xFFFF, nB = T32(pg + 2) >> 16;
             const uint32_t dA = T32(pg + 4), dB = T32(pg + 6);
             if (n < 1 || n > (uint32_t)kSharedRows) return fail("program rows", s, q, n);
+            if (dB != 0xFFFFFFFFu && nA != nB) return fail("unequal halves", s, nA, nB);
+            if (dB == 0xFFFFFFFFu && nA) return fail("micro-ops without chain B", s, q, nA);
             // both half-chains of every lane of the chunk
             for (uint32_t half = 0; half < 2; half++) {
               const uint32_t d0 = half ? dB : dA;
@@ -155,9 +164,11 @@ int main(int argc, char **argv) {
               uint32_t lo[32] = {0}, hi[32] = {0};
               for (uint32_t lane = 0; lane < 32; lane++) {
                 const uint32_t g = std::min(c * 31 + lane, ng - 1);  // lanes past the series
-                for (uint32_t e = 0; e < n; e++) {
+                for (uint32_t e = 0; e < (uint32_t)kSharedRows; e++) {
                   uint32_t w;
-                  if (!rd(T32(pg + 8 + 16 * half + 2 * e), g, w)) return fail("copy read", s, q, e);
+                  const uint32_t ob = T32(pg + 8 + 16 * half + 2 * e);
+                  if (e >= n && ob != 4 * zrow) return fail("row past n not the zero row", s, q, e);
+                  if (!rd(ob, g, w)) return fail("copy read", s, q, e);
                   lo[lane] += prmt4140(w);
                   hi[lane] += prmt4342(w);
                 }
