@@ -250,7 +250,8 @@ def bench_batched(torch, device: int, reps: int = 3, count: int = 40):
     return {"value": units / t_batch, "unit": UNIT, "ms_per_batch": t_batch * 1e3,
             "plain_sequential_value": units / t_plain, "plain_sequential_ms": t_plain * 1e3,
             "speedup_vs_plain": t_plain / t_batch, "beams": count, "tiles": info["tiles"],
-            "persistent_ctas": info["grid"], "bit_exact_vs_plain": exact,
+            "persistent_ctas": info["grid"], "tile": info.get("tile"),
+            "bit_exact_vs_plain": exact,
             "launch": "one persistent kernel replayed from a CUDA graph",
             "workload": "40 beams: 384/1536 ch, 8192-32768 samples, 512-4096 DMs, DM step "
                         "0.1-0.5, 2/4/8-bit uniform input, 5% zapped"}

@@ -408,7 +408,12 @@ class Batch:
     def info(self) -> dict:
         p, t, g = C.c_uint32(), C.c_uint32(), C.c_uint32()
         check(lib().dd_batch_info(self._h, C.byref(p), C.byref(t), C.byref(g)))
-        return {"problems": p.value, "tiles": t.value, "grid": g.value}
+        info = {"problems": p.value, "tiles": t.value, "grid": g.value}
+        if t.value:
+            sh = C.c_int(0)
+            check(lib().dd_batch_shared(self._h, C.byref(sh)))
+            info["tile"] = "shared" if sh.value else "direct"
+        return info
 
     def close(self) -> None:
         if self._h:

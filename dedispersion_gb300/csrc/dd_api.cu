@@ -278,6 +278,9 @@ struct dd_plan {
   // Created without a configuration: a shape that the default shared kernel
   // cannot take runs on the default direct kernel instead.
   bool auto_kernel = false;
+  // Shared memory per block kept free for a caller's kernel (the batch
+  // kernel's own static shared memory).
+  uint32_t smem_reserve = 0;
 };
 
 namespace {
@@ -402,7 +405,7 @@ dd_status rebuild(dd_plan *p) {
       return fail(DD_ERR_UNSUPPORTED, "kernel %s computes single-step 1/2/4/8-bit input only",
                   k.name);
     // One CTA per SM: the whole opt-in shared memory of a block.
-    const size_t budget = (size_t)dev_max;
+    const size_t budget = (size_t)dev_max - p->smem_reserve;
     (void)sm_max;
     const std::string why = dd::build_shared_tables(k, p->delay_shift, d.first_dm, d.dm_step,
                                                     d.nr_dms, p->bits, budget, &p->shared);
@@ -544,6 +547,15 @@ dd_status rebuild_auto(dd_plan *p) {
 namespace dd {
 // Lets other translation units of the library report through dd_last_error.
 void set_last_error(const char *message) { g_error = message; }
+
+// Keep `bytes` of a block's shared memory free (before the tables are built).
+void plan_set_smem_reserve(dd_plan *p, uint32_t bytes) { p->smem_reserve = bytes; }
+
+// Whether the plan's tables are built (a deferred error leaves them unbuilt).
+bool plan_ready(const dd_plan *p) { return p->ready; }
+
+// Family of the kernel the plan runs.
+int plan_family(const dd_plan *p) { return p->kinfo->family; }
 
 // The kernel arguments of one run of `p` on the given device buffers; also
 // the rows each group sums (the cost of one of its tiles).

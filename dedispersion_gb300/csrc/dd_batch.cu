@@ -9,6 +9,9 @@
 // next tile from the work counter and computes it with the same tile routine
 // as the plain kernel, so results equal the plain path's bit for bit.
 //
+// Two tile routines: the shared-partial-sum tile (the plain path's default)
+// when every problem's tables fit it, else the direct swar8 tile.
+//
 // There is no counterpart in the reference (its test driver launches one
 // kernel per configuration and beam set, src/DedispersionTest.cpp:366-399).
 #include <cuda_runtime.h>
@@ -22,12 +25,16 @@
 
 #include "../../include/dedisp_gb300.h"
 #include "dd_device.cuh"
+#include "dd_shared.cuh"
 
 namespace dd {
 void set_last_error(const char *message);
 // Plan internals shared with dd_api.cu.
 dd_status plan_problem(const dd_plan *plan, const void *d_input, float *d_output,
                        ProblemDesc *problem, uint64_t *rows_per_group);
+void plan_set_smem_reserve(dd_plan *p, uint32_t bytes);
+bool plan_ready(const dd_plan *p);
+int plan_family(const dd_plan *p);
 }
 
 namespace {
@@ -84,6 +91,55 @@ __global__ void __launch_bounds__(kThreads, 2) batch_kernel(const BatchDesc B) {
   }
 }
 
+// The shared-partial-sum batch tile: the plain path's default configuration.
+constexpr int kSNW = 4, kSND = 4, kSTY = 16;
+constexpr int kSThreads = 32 * kSTY;
+constexpr uint32_t kSharedReserve = 1024;  // static shared memory of the kernel
+
+__global__ void __launch_bounds__(kSThreads, 1) batch_shared_kernel(const BatchDesc B) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  __shared__ dd::ProblemDesc sP;
+  __shared__ uint32_t s_tile, s_local;
+  if (threadIdx.x == 0) {
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
+    for (int r = 0; r < dd::kSharedSlots; ++r) dd::mbar_init(bars + r, blockDim.x);
+    dd::fence_mbar_init();
+  }
+  uint32_t sc = 0;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const uint32_t t = atomicAdd(B.counter, 1u);
+      s_tile = t;
+      if (t < B.total_tiles) {
+        uint32_t lo = 0, hi = B.nproblems;  // last p with tile_start[p] <= t
+        while (hi - lo > 1) {
+          const uint32_t mid = (lo + hi) / 2;
+          if (B.tile_start[mid] <= t) lo = mid; else hi = mid;
+        }
+        sP = B.problems[lo];
+        s_local = t - B.tile_start[lo];
+      }
+    }
+    __syncthreads();
+    if (s_tile >= B.total_tiles) break;
+    // This problem's layout inside the batch's allocation (the largest of
+    // any problem's): its zero series and zero row are cleared per tile, as
+    // the previous tile may have used that memory otherwise.
+    const dd::SharedLayout L =
+        dd::make_shared_layout(sP.cw, sP.psw, sP.slots, sP.table_bytes, sP.bits);
+    uint32_t *zero = reinterpret_cast<uint32_t *>(smem + L.off_part) + L.zero_word;
+    for (uint32_t w = threadIdx.x; w < sP.psw; w += blockDim.x) zero[w] = 0;
+    uint32_t *zrow = reinterpret_cast<uint32_t *>(smem + L.off_copy) + L.zero_copy;
+    for (uint32_t w = threadIdx.x; w < sP.cw; w += blockDim.x) zrow[w] = 0;
+    uint32_t g, dtile, ttile;
+    dd::decode_tile(sP, s_local, g, dtile, ttile);
+    const bool ok =
+        dd::shared8_tile<kSNW, kSND, kSTY>(sP, g, sP.groups[g], dtile, ttile, smem, L, sc);
+    if (!ok) break;  // uniform: decided by a block-wide vote inside the tile
+    __syncthreads();  // everyone is done with sP and s_tile
+  }
+}
+
 dd_status fail(dd_status code, const char *fmt, ...) {
   char buf[512];
   va_list ap;
@@ -111,7 +167,9 @@ dd_status cuda_fail(cudaError_t e, const char *what) {
 
 struct dd_batch {
   int device = 0;
-  std::vector<dd_plan *> plans;
+  std::vector<dd_plan *> plans;         // direct-tile plans (always built)
+  std::vector<dd_plan *> shared_plans;  // shared-tile plans (NULL: shape does not fit)
+  bool shared = false;                  // committed with the shared tile
   std::vector<const void *> inputs;
   std::vector<float *> outputs;
   // committed state
@@ -144,7 +202,10 @@ void release(dd_batch *b) {
 // Enqueue [counter reset, kernel] on `s`.
 dd_status enqueue(dd_batch *b, cudaStream_t s) {
   DDB_CUDA(cudaMemsetAsync(b->d_scratch, 0, sizeof(uint32_t), s), "reset work counter");
-  batch_kernel<<<b->grid, kThreads, b->smem, s>>>(b->desc);
+  if (b->shared)
+    batch_shared_kernel<<<b->grid, kSThreads, b->smem, s>>>(b->desc);
+  else
+    batch_kernel<<<b->grid, kThreads, b->smem, s>>>(b->desc);
   DDB_CUDA(cudaGetLastError(), "launch batch kernel");
   return DD_OK;
 }
@@ -187,9 +248,26 @@ dd_status dd_batch_add(dd_batch *b, const dd_observation *obs, uint32_t input_bi
     dd_plan_destroy(p);
     return st;
   }
+  // The same problem on the shared tile, if its tables fit.
+  dd_conf sconf{0, 1, (uint32_t)dd::kSharedRows, 32, kSTY, 1, 2 * kSNW, kSND,
+                (uint32_t)dd::kSharedRows};
+  dd_plan *q = nullptr;
+  if (dd_plan_create(&q, obs, DD_SINGLE_STEP, input_bits, padding, &sconf, b->device) == DD_OK) {
+    dd::plan_set_smem_reserve(q, kSharedReserve);
+    bool good = dd_plan_set_shifts(q, shifts, obs->nr_channels) == DD_OK &&
+                dd_plan_set_zapped(q, zapped, obs->nr_channels) == DD_OK &&
+                dd_plan_set_beam_mapping(q, beam_mapping, (size_t)obs->nr_synthesized_beams *
+                                                              lay.mapping_row_elems) == DD_OK;
+    good = good && dd::plan_ready(q) && dd::plan_family(q) == dd::kFamilyShared8;
+    if (!good) {
+      dd_plan_destroy(q);
+      q = nullptr;
+    }
+  }
   if (b->committed) release(b);
   if (index) *index = (uint32_t)b->plans.size();
   b->plans.push_back(p);
+  b->shared_plans.push_back(q);
   b->inputs.push_back(d_input);
   b->outputs.push_back(d_output);
   return DD_OK;
@@ -200,10 +278,13 @@ dd_status dd_batch_commit(dd_batch *b) {
   if (b->plans.empty()) return fail(DD_ERR_INVALID_ARGUMENT, "batch is empty");
   release(b);
   const size_t n = b->plans.size();
+  b->shared = std::all_of(b->shared_plans.begin(), b->shared_plans.end(),
+                          [](dd_plan *q) { return q != nullptr; });
   std::vector<dd::ProblemDesc> probs(n);
   std::vector<uint64_t> rows(n);
   for (size_t i = 0; i < n; i++) {
-    dd_status st = dd::plan_problem(b->plans[i], b->inputs[i], b->outputs[i], &probs[i], &rows[i]);
+    dd_status st = dd::plan_problem(b->shared ? b->shared_plans[i] : b->plans[i], b->inputs[i],
+                                    b->outputs[i], &probs[i], &rows[i]);
     if (st) return st;
   }
   // Uniform slots sized for the largest raw row and copy of any problem; each
@@ -248,15 +329,27 @@ dd_status dd_batch_commit(dd_batch *b) {
   DDB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device), "query SMs");
   // The kernel's own static shared memory (the problem descriptor) comes out
   // of the same per-block budget.
+  const void *kfn = b->shared ? reinterpret_cast<const void *>(&batch_shared_kernel)
+                              : reinterpret_cast<const void *>(&batch_kernel);
+  const int threads = b->shared ? kSThreads : kThreads;
+  if (b->shared) {
+    L.total = 0;
+    for (auto &P : probs)
+      L.total = std::max(L.total, dd::make_shared_layout(P.cw, P.psw, P.slots, P.table_bytes,
+                                                         P.bits).total);
+  }
   cudaFuncAttributes fa{};
-  DDB_CUDA(cudaFuncGetAttributes(&fa, batch_kernel), "query kernel attributes");
+  DDB_CUDA(cudaFuncGetAttributes(&fa, kfn), "query kernel attributes");
   const size_t static_smem = fa.sharedSizeBytes;
+  if (b->shared && static_smem > kSharedReserve)
+    return fail(DD_ERR_UNSUPPORTED, "batch kernel keeps %zu bytes of static shared memory",
+                static_smem);
   if (L.total + static_smem > (size_t)smem_max)
     return fail(DD_ERR_UNSUPPORTED, "batch window needs %u bytes of shared memory", L.total);
-  DDB_CUDA(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  DDB_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 smem_max - (int)static_smem),
            "set kernel shared memory");
-  DDB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, kThreads, L.total),
+  DDB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, threads, L.total),
            "occupancy");
   if (per_sm < 1) return fail(DD_ERR_UNSUPPORTED, "batch kernel does not fit on an SM");
   b->smem = L.total;
@@ -325,11 +418,20 @@ dd_status dd_batch_info(const dd_batch *b, uint32_t *problems, uint32_t *tiles, 
   return DD_OK;
 }
 
+dd_status dd_batch_shared(const dd_batch *b, int *shared) {
+  if (!b || !shared) return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (!b->committed) return fail(DD_ERR_INVALID_ARGUMENT, "batch is not committed");
+  *shared = b->shared ? 1 : 0;
+  return DD_OK;
+}
+
 dd_status dd_batch_destroy(dd_batch *b) {
   if (!b) return DD_OK;
   cudaSetDevice(b->device);
   release(b);
   for (dd_plan *p : b->plans) dd_plan_destroy(p);
+  for (dd_plan *q : b->shared_plans)
+    if (q) dd_plan_destroy(q);
   delete b;
   return DD_OK;
 }

@@ -307,6 +307,9 @@ dd_status dd_batch_check(dd_batch *batch, void *stream);
 /* Problems, tiles and persistent CTAs of a committed batch. */
 dd_status dd_batch_info(const dd_batch *batch, uint32_t *problems,
                         uint32_t *tiles, uint32_t *grid);
+/* 1 if a committed batch runs the shared-partial-sum tile (every problem's
+ * tables fit it), 0 if the direct tile. */
+dd_status dd_batch_shared(const dd_batch *batch, int *shared);
 dd_status dd_batch_destroy(dd_batch *batch);
 
 /* ---- streams: one beam of a real-time batch stream ---------------------- */
