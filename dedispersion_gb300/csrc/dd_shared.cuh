@@ -97,6 +97,15 @@ __device__ __forceinline__ void sts_v2(uint32_t addr, uint32_t a, uint32_t b) {
                : "memory");
 }
 
+// Predicated store (no branch): writes only where `on` is non-zero.
+__device__ __forceinline__ void sts_v2_if(uint32_t on, uint32_t addr, uint32_t a, uint32_t b) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %3, 0;\n\t"
+      "@p st.shared.v2.b32 [%0], {%1, %2};\n\t}" ::"r"(addr),
+      "r"(a), "r"(b), "r"(on)
+      : "memory");
+}
+
 __device__ __forceinline__ uint2 lds_v2(uint32_t addr) {
   uint2 v;
   asm volatile("ld.shared.v2.b32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "r"(addr));
@@ -293,10 +302,12 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
       const uint32_t g = (item & 0xFFu) * 31u + tx;
       // Lanes past the series compute its last group again and store nothing.
       const uint32_t gb = copy_s + 4u * (g < ng ? g : ng - 1u);
-      // Stores of lanes that keep nothing go to the dummy series.
-      const bool keep = tx < 31 && g < ng;
+      // Lane 31 and lanes past the series store nothing (predicated stores);
+      // neither does a micro-op whose vector is not complete yet (dst = the
+      // dummy series).
+      const uint32_t keep = (tx < 31 && g < ng) ? 1u : 0u;
       const uint32_t pg = part_s + 8u * g;
-      const uint32_t junk = part_s + 4u * L.dummy_word + 8u * tx;
+      const uint32_t dummy = 4u * L.dummy_word;
       // lo = (P[4g], P[4g+1]), hi = (P[4g+2], P[4g+3]) as 16-bit lanes.
       uint32_t loA = 0, hiA = 0, loB = 0, hiB = 0;
       auto rows = [&](const uint32_t *offs, uint32_t &lo, uint32_t &hi) {
@@ -312,9 +323,10 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
       };
       auto store = [&](uint32_t dst, uint32_t lo, uint32_t hi) {
         const uint32_t nlo = __shfl_down_sync(0xffffffffu, lo, 1);
-        const uint32_t at = keep ? pg + dst : junk;
-        sts_v2(at, lo, hi);
-        sts_v2(at + 4u * psw, __byte_perm(lo, hi, 0x5432), __byte_perm(hi, nlo, 0x5432));
+        const uint32_t on = keep & (dst != dummy ? 1u : 0u);
+        sts_v2_if(on, pg + dst, lo, hi);
+        sts_v2_if(on, pg + dst + 4u * psw, __byte_perm(lo, hi, 0x5432),
+                  __byte_perm(hi, nlo, 0x5432));
       };
       auto step = [&](const uint4 &u, uint32_t &lo, uint32_t &hi) {
         const uint32_t wo = lds_u32(gb + u.x);
