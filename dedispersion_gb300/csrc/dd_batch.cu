@@ -10,7 +10,9 @@
 // as the plain kernel, so results equal the plain path's bit for bit.
 //
 // Two tile routines: the shared-partial-sum tile (the plain path's default)
-// when every problem's tables fit it, else the direct swar8 tile.
+// when every problem's tables fit it, else the direct swar8 tile.  The
+// shared-tile kernel takes its tiles in a fixed round-robin order over the
+// longest-first list instead of from the work counter.
 //
 // There is no counterpart in the reference (its test driver launches one
 // kernel per configuration and beam set, src/DedispersionTest.cpp:366-399).
@@ -96,47 +98,53 @@ constexpr int kSNW = 4, kSND = 4, kSTY = 16;
 constexpr int kSThreads = 32 * kSTY;
 constexpr uint32_t kSharedReserve = 1024;  // static shared memory of the kernel
 
-__global__ void __launch_bounds__(kSThreads, 1) batch_shared_kernel(const BatchDesc B) {
+// A shared-tile batch passes its problems by value in the kernel parameters
+// (up to 32 KB on this architecture): tile code then reads a problem's fields
+// from the constant bank, as the plain kernel does, instead of from shared
+// memory on every use.
+constexpr uint32_t kSharedBatchMax = 160;
+
+struct SharedBatchParams {
+  uint32_t nproblems;
+  uint32_t total_tiles;
+  uint32_t tile_start[kSharedBatchMax + 1];  // prefix sums of tiles
+  dd::ProblemDesc problems[kSharedBatchMax];  // longest tiles first
+};
+static_assert(sizeof(SharedBatchParams) <= 32000, "kernel parameters are limited to 32 KB");
+
+// Tiles are taken in a fixed round-robin order over the longest-first list
+// (CTA c computes tiles c, c + grid, ...): no work counter.
+__global__ void __launch_bounds__(kSThreads, 1)
+    batch_shared_kernel(const __grid_constant__ SharedBatchParams B) {
   extern __shared__ __align__(128) uint8_t smem[];
-  __shared__ dd::ProblemDesc sP;
-  __shared__ uint32_t s_tile, s_local;
   if (threadIdx.x == 0) {
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
     for (int r = 0; r < dd::kSharedSlots; ++r) dd::mbar_init(bars + r, blockDim.x);
     dd::fence_mbar_init();
   }
+  __syncthreads();
   uint32_t sc = 0;
-  for (;;) {
-    if (threadIdx.x == 0) {
-      const uint32_t t = atomicAdd(B.counter, 1u);
-      s_tile = t;
-      if (t < B.total_tiles) {
-        uint32_t lo = 0, hi = B.nproblems;  // last p with tile_start[p] <= t
-        while (hi - lo > 1) {
-          const uint32_t mid = (lo + hi) / 2;
-          if (B.tile_start[mid] <= t) lo = mid; else hi = mid;
-        }
-        sP = B.problems[lo];
-        s_local = t - B.tile_start[lo];
-      }
+  for (uint32_t t = blockIdx.x; t < B.total_tiles; t += gridDim.x) {
+    uint32_t lo = 0, hi = B.nproblems;  // last p with tile_start[p] <= t
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) / 2;
+      if (B.tile_start[mid] <= t) lo = mid; else hi = mid;
     }
-    __syncthreads();
-    if (s_tile >= B.total_tiles) break;
+    const dd::ProblemDesc &P = B.problems[lo];
     // This problem's layout inside the batch's allocation (the largest of
     // any problem's): its zero series and zero row are cleared per tile, as
     // the previous tile may have used that memory otherwise.
-    const dd::SharedLayout L =
-        dd::make_shared_layout(sP.cw, sP.psw, sP.slots, sP.table_bytes, sP.bits);
+    const dd::SharedLayout L = dd::make_shared_layout(P.cw, P.psw, P.slots, P.table_bytes, P.bits);
     uint32_t *zero = reinterpret_cast<uint32_t *>(smem + L.off_part) + L.zero_word;
-    for (uint32_t w = threadIdx.x; w < sP.psw; w += blockDim.x) zero[w] = 0;
+    for (uint32_t w = threadIdx.x; w < P.psw; w += blockDim.x) zero[w] = 0;
     uint32_t *zrow = reinterpret_cast<uint32_t *>(smem + L.off_copy) + L.zero_copy;
-    for (uint32_t w = threadIdx.x; w < sP.cw; w += blockDim.x) zrow[w] = 0;
+    for (uint32_t w = threadIdx.x; w < P.cw; w += blockDim.x) zrow[w] = 0;
     uint32_t g, dtile, ttile;
-    dd::decode_tile(sP, s_local, g, dtile, ttile);
+    dd::decode_tile(P, t - B.tile_start[lo], g, dtile, ttile);
     const bool ok =
-        dd::shared8_tile<kSNW, kSND, kSTY>(sP, g, sP.groups[g], dtile, ttile, smem, L, sc);
+        dd::shared8_tile<kSNW, kSND, kSTY>(P, g, P.groups[g], dtile, ttile, smem, L, sc);
     if (!ok) break;  // uniform: decided by a block-wide vote inside the tile
-    __syncthreads();  // everyone is done with sP and s_tile
+    __syncthreads();  // the tile's last reads of shared memory are done
   }
 }
 
@@ -178,6 +186,7 @@ struct dd_batch {
   uint32_t *d_tile_start = nullptr;
   uint32_t *d_scratch = nullptr;  // [0] work counter, [1] status word
   BatchDesc desc{};
+  SharedBatchParams *sparams = nullptr;  // shared-tile launch parameters
   size_t smem = 0;
   unsigned grid = 0;
   cudaGraph_t graph = nullptr;
@@ -203,7 +212,7 @@ void release(dd_batch *b) {
 dd_status enqueue(dd_batch *b, cudaStream_t s) {
   DDB_CUDA(cudaMemsetAsync(b->d_scratch, 0, sizeof(uint32_t), s), "reset work counter");
   if (b->shared)
-    batch_shared_kernel<<<b->grid, kSThreads, b->smem, s>>>(b->desc);
+    batch_shared_kernel<<<b->grid, kSThreads, b->smem, s>>>(*b->sparams);
   else
     batch_kernel<<<b->grid, kThreads, b->smem, s>>>(b->desc);
   DDB_CUDA(cudaGetLastError(), "launch batch kernel");
@@ -278,7 +287,8 @@ dd_status dd_batch_commit(dd_batch *b) {
   if (b->plans.empty()) return fail(DD_ERR_INVALID_ARGUMENT, "batch is empty");
   release(b);
   const size_t n = b->plans.size();
-  b->shared = std::all_of(b->shared_plans.begin(), b->shared_plans.end(),
+  b->shared = n <= kSharedBatchMax &&
+              std::all_of(b->shared_plans.begin(), b->shared_plans.end(),
                           [](dd_plan *q) { return q != nullptr; });
   std::vector<dd::ProblemDesc> probs(n);
   std::vector<uint64_t> rows(n);
@@ -365,6 +375,14 @@ dd_status dd_batch_commit(dd_batch *b) {
                       cudaMemcpyHostToDevice), "upload problems");
   DDB_CUDA(cudaMemcpy(b->d_tile_start, start.data(), (n + 1) * sizeof(uint32_t),
                       cudaMemcpyHostToDevice), "upload tile table");
+  if (b->shared) {
+    if (!b->sparams) b->sparams = new SharedBatchParams();
+    std::memset(b->sparams, 0, sizeof(SharedBatchParams));
+    b->sparams->nproblems = (uint32_t)n;
+    b->sparams->total_tiles = (uint32_t)total;
+    std::copy(start.begin(), start.end(), b->sparams->tile_start);
+    std::copy(sorted.begin(), sorted.end(), b->sparams->problems);
+  }
   b->desc.problems = b->d_problems;
   b->desc.tile_start = b->d_tile_start;
   b->desc.counter = b->d_scratch;
@@ -432,6 +450,7 @@ dd_status dd_batch_destroy(dd_batch *b) {
   for (dd_plan *p : b->plans) dd_plan_destroy(p);
   for (dd_plan *q : b->shared_plans)
     if (q) dd_plan_destroy(q);
+  delete b->sparams;
   delete b;
   return DD_OK;
 }
