@@ -68,6 +68,9 @@ def parse():
                     help="skip the 40-beam batched measurement")
     ap.add_argument("--no-served", action="store_true",
                     help="skip the 12-beam serving measurement")
+    ap.add_argument("--kernel", default=None,
+                    help="registry name of the tile configuration to run (default: the "
+                         "library's default for the workload)")
     ap.add_argument("--kernel-only", action="store_true",
                     help="run only the warm-up and timed kernel launches (the command ncu "
                          "captures); prints the device-resident figure alone")
@@ -362,7 +365,12 @@ def main():
     S, D = obs.getNrSamplesPerBatch(), obs.getNrDMs()
     live = int((zapped[:1536] == 0).sum())
     lay = dd.layout(obs, dd.DD_SINGLE_STEP, 8, PADDING, shifts)
-    plan = dd.Plan(obs, dd.DD_SINGLE_STEP, 8, PADDING, device=local)
+    kidx = None
+    if args.kernel:
+        kidx = next((k.index for k in dd.kernels() if k.name == args.kernel), None)
+        if kidx is None:
+            raise SystemExit(f"no compiled configuration named {args.kernel}")
+    plan = dd.Plan(obs, dd.DD_SINGLE_STEP, 8, PADDING, device=local, kernel=kidx)
     plan.setShifts(shifts)
     plan.setZappedChannels(zapped)
     plan.setBeamMapping(mapping)
