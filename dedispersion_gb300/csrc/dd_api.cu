@@ -281,6 +281,9 @@ struct dd_plan {
   // Shared memory per block kept free for a caller's kernel (the batch
   // kernel's own static shared memory).
   uint32_t smem_reserve = 0;
+  // Tables changed since the last build: setters only record their table;
+  // the first use (run, timing, queries) builds once.
+  bool dirty = false;
 };
 
 namespace {
@@ -543,6 +546,23 @@ dd_status rebuild_auto(dd_plan *p) {
 }
 
 }  // namespace
+extern "C" {
+namespace {
+dd_status rebuild_deferred(dd_plan *p);  // defined with the setters below
+}  // namespace
+}
+namespace {
+
+// Build the tables if a setter changed them since the last build.  Plans are
+// logically const for their queries; the build is a cache.
+dd_status ensure_built(const dd_plan *cp) {
+  dd_plan *p = const_cast<dd_plan *>(cp);
+  if (!p->dirty) return DD_OK;
+  p->dirty = false;
+  return rebuild_deferred(p);
+}
+
+}  // namespace
 
 namespace dd {
 // Lets other translation units of the library report through dd_last_error.
@@ -552,15 +572,19 @@ void set_last_error(const char *message) { g_error = message; }
 void plan_set_smem_reserve(dd_plan *p, uint32_t bytes) { p->smem_reserve = bytes; }
 
 // Whether the plan's tables are built (a deferred error leaves them unbuilt).
-bool plan_ready(const dd_plan *p) { return p->ready; }
+bool plan_ready(const dd_plan *p) { return ensure_built(p) == DD_OK && p->ready; }
 
 // Family of the kernel the plan runs.
-int plan_family(const dd_plan *p) { return p->kinfo->family; }
+int plan_family(const dd_plan *p) {
+  (void)ensure_built(p);
+  return p->kinfo->family;
+}
 
 // The kernel arguments of one run of `p` on the given device buffers; also
 // the rows each group sums (the cost of one of its tiles).
 dd_status plan_problem(const dd_plan *p, const void *d_input, float *d_output,
                        ProblemDesc *out, uint64_t *rows_per_group) {
+  if (dd_status st = ensure_built(p)) return st;
   if (!p->ready)
     return fail(DD_ERR_INVALID_ARGUMENT, p->have_shifts ? "plan tables are invalid: %s"
                                                         : "plan has no shift table%s",
@@ -869,7 +893,9 @@ dd_status dd_plan_set_shifts(dd_plan *p, const float *shifts, size_t n) {
   if (n < need) return fail(DD_ERR_INVALID_ARGUMENT, "shift table has %zu entries, needs %zu", n, need);
   p->shifts.assign(shifts, shifts + need);
   p->have_shifts = true;
-  return rebuild_deferred(p);
+  p->dirty = true;
+  p->ready = false;
+  return DD_OK;
 }
 
 dd_status dd_plan_set_zapped(dd_plan *p, const uint32_t *zapped, size_t n) {
@@ -878,7 +904,9 @@ dd_status dd_plan_set_zapped(dd_plan *p, const uint32_t *zapped, size_t n) {
   if (n < p->obs.nr_channels)
     return fail(DD_ERR_INVALID_ARGUMENT, "zapped mask has %zu entries, needs %u", n, p->obs.nr_channels);
   p->zapped.assign(zapped, zapped + p->obs.nr_channels);
-  return rebuild_deferred(p);
+  p->dirty = true;
+  p->ready = false;
+  return DD_OK;
 }
 
 dd_status dd_plan_set_beam_mapping(dd_plan *p, const uint32_t *mapping, size_t n) {
@@ -887,7 +915,9 @@ dd_status dd_plan_set_beam_mapping(dd_plan *p, const uint32_t *mapping, size_t n
   size_t need = (size_t)p->obs.nr_synthesized_beams * p->dims.mapping_row;
   if (n < need) return fail(DD_ERR_INVALID_ARGUMENT, "beam mapping has %zu entries, needs %zu", n, need);
   p->mapping.assign(mapping, mapping + need);
-  return rebuild_deferred(p);
+  p->dirty = true;
+  p->ready = false;
+  return DD_OK;
 }
 
 dd_status dd_plan_run(dd_plan *p, const void *d_input, float *d_output, void *stream) {
@@ -962,6 +992,10 @@ dd_status dd_plan_launches(const dd_plan *p, uint32_t *launches) {
 }
 
 dd_status dd_plan_get_conf(const dd_plan *p, dd_conf *conf) {
+  if (p) {
+    dd_status st = ensure_built(p);
+    if (st) return st;
+  }
   if (!p || !conf) return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
   *conf = conf_of(*p->kinfo);
   return DD_OK;
@@ -969,6 +1003,7 @@ dd_status dd_plan_get_conf(const dd_plan *p, dd_conf *conf) {
 
 dd_status dd_plan_adds(const dd_plan *p, uint64_t *adds) {
   if (!p || !adds) return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (dd_status st = ensure_built(p)) return st;
   if (!p->ready)
     return fail(DD_ERR_INVALID_ARGUMENT, p->have_shifts ? "plan tables are invalid: %s"
                                                         : "plan has no shift table%s",

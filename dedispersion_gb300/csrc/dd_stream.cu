@@ -254,6 +254,11 @@ dd_status dd_stream_create(dd_stream **out, const dd_observation *obs, int subba
     if (!st) st = dd_plan_set_shifts(s->plan2, shifts_step_two, g.two.nr_subbands);
     if (!st) st = dd_plan_set_beam_mapping(s->plan2, map.data(), map.size());
   }
+  // Build the plans' tables now (they are built on first use), so that the
+  // push recorded as a graph below launches only kernels.
+  uint64_t adds = 0;
+  if (!st) st = dd_plan_adds(s->plan1, &adds);
+  if (!st && s->subband) st = dd_plan_adds(s->plan2, &adds);
   if (st) return bail(st);
   // buffers
   s->in_row_bytes = bytes_of(S, input_bits);
