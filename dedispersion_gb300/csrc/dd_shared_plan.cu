@@ -62,9 +62,14 @@ struct Window {
     }
     *maxrel = mr;
     if (mr > kRelMax) return UINT32_MAX;
-    uniq = key;
+    // Neighbouring DMs mostly share a vector: drop runs first, then sort the
+    // few keys left.
+    uniq.clear();
+    for (uint32_t j = 0; j < DB; j++)
+      if (j == 0 || key[j] != key[j - 1]) uniq.push_back(key[j]);
     std::sort(uniq.begin(), uniq.end());
-    return (uint32_t)(std::unique(uniq.begin(), uniq.end()) - uniq.begin());
+    uniq.erase(std::unique(uniq.begin(), uniq.end()), uniq.end());
+    return (uint32_t)uniq.size();
   }
 };
 
@@ -83,17 +88,32 @@ std::vector<Sub> cut_tile(const std::vector<float> &row_shift, const float *dv, 
   auto delay = [&](uint32_t r, uint32_t j) { return static_cast<uint32_t>(dv[j] * row_shift[r]); };
   uint32_t r = 0;
   while (r < K) {
-    uint32_t n = 0, mr = 0;
-    for (uint32_t m = 1; m <= (uint32_t)kSharedRows && r + m <= K; m++) {
-      for (uint32_t j = 0; j < DB; j++) w.dl[(m - 1) * DB + j] = delay(r + m - 1, j);
-      const uint32_t nv = w.count(m, &mr);
-      if (m > 1 && (nv == UINT32_MAX || nv > nv_cap)) break;
-      n = m;
+    // The largest subgroup that fits: the vector count and the largest
+    // relative delay only grow with the rows, so try all rows first and
+    // search downwards only when they do not fit.
+    const uint32_t mmax = std::min<uint32_t>(kSharedRows, K - r);
+    for (uint32_t e = 0; e < mmax; e++)
+      for (uint32_t j = 0; j < DB; j++) w.dl[e * DB + j] = delay(r + e, j);
+    uint32_t mr = 0, counted = 0, nv = 0;  // the Window holds the count of `counted` rows
+    auto fits = [&](uint32_t m) {
+      nv = w.count(m, &mr);
+      counted = m;
+      return nv != UINT32_MAX && nv <= nv_cap;
+    };
+    uint32_t n = mmax;
+    if (!fits(mmax)) {
+      uint32_t lo = 1, hi = mmax;  // fits(lo) holds (one row, one vector), fits(hi) does not
+      while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (fits(mid)) lo = mid; else hi = mid;
+      }
+      n = lo;
     }
     Sub s;
     s.r0 = r;
     s.n = n;
-    const uint32_t nv = w.count(n, &s.maxrel);
+    if (counted != n) fits(n);
+    s.maxrel = mr;
     uint32_t bmin = UINT32_MAX, bmax = 0;
     for (uint32_t j = 0; j < DB; j++) {
       bmin = std::min(bmin, w.base[j]);
