@@ -345,6 +345,21 @@ class KernelEntry:
     conf: DedispersionConf
 
 
+DM_STATS = np.dtype([("mean", np.float64), ("stddev", np.float64), ("snr", np.float64),
+                     ("peak", np.float32), ("peak_sample", np.uint32)])
+
+
+def dm_stats(accum, samples: int) -> np.ndarray:
+    """Mean, standard deviation, S/N, peak and peak sample of each output row
+    from the accumulators :meth:`Plan.run_stats` fills (host array of
+    ``rows x 3`` uint64)."""
+    acc = np.ascontiguousarray(np.asarray(accum, dtype=np.uint64).reshape(-1, 3))
+    out = np.zeros(len(acc), dtype=DM_STATS)
+    check(lib().dd_dm_stats_from_accum(acc.ctypes.data_as(C.c_void_p), len(acc), int(samples),
+                                       out.ctypes.data_as(C.c_void_p)))
+    return out
+
+
 def kernels() -> list[KernelEntry]:
     """Every compiled tile configuration (the tuner's search space)."""
     out = []
@@ -476,6 +491,15 @@ class Plan:
         c = DdConf()
         check(lib().dd_plan_get_conf(self._h, C.byref(c)))
         return DedispersionConf.from_c(c)
+
+    def run_stats(self, d_input, d_output, d_accum, stream=None) -> None:
+        """run() plus detection statistics of the output in ``d_accum`` (device
+        buffer of 3 x uint64 per output row: sum, sum of squares, peak key;
+        see :func:`dm_stats`)."""
+        check(lib().dd_plan_run_stats(self._h, C.c_void_p(_devptr(d_input)),
+                                      C.c_void_p(_devptr(d_output)),
+                                      C.c_void_p(_devptr(d_accum)),
+                                      C.c_void_p(_stream(stream))))
 
     def adds(self) -> int:
         """Integer adds one run performs (tile padding included)."""

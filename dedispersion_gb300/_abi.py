@@ -124,6 +124,8 @@ SIGNATURES = {
     "dd_plan_launches": (C.c_int, [_P, _U32P]),
     "dd_plan_get_conf": (C.c_int, [_P, _CONF]),
     "dd_plan_adds": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    "dd_plan_run_stats": (C.c_int, [_P, _P, _P, _P, _P]),
+    "dd_dm_stats_from_accum": (C.c_int, [_P, C.c_size_t, C.c_uint32, _P]),
     "dd_plan_destroy": (C.c_int, [_P]),
     "dd_batch_create": (C.c_int, [C.POINTER(_P), C.c_int]),
     "dd_batch_add": (C.c_int, [_P, _OBS, C.c_uint32, C.c_uint32, _F32P, _U32P, _U32P, _P, _P,

@@ -565,6 +565,8 @@ dd_status ensure_built(const dd_plan *cp) {
 }  // namespace
 
 namespace dd {
+cudaError_t launch_row_stats(const ProblemDesc &P, unsigned long long *accum, uint32_t rows,
+                             cudaStream_t stream);
 // Lets other translation units of the library report through dd_last_error.
 void set_last_error(const char *message) { g_error = message; }
 
@@ -931,6 +933,33 @@ dd_status dd_plan_run(dd_plan *p, const void *d_input, float *d_output, void *st
   if (!g.ok) return fail(DD_ERR_CUDA, "cannot select device %d", p->device);
   p->kinfo->launch(P, (unsigned)tiles, p->smem, static_cast<cudaStream_t>(stream));
   DD_CUDA(cudaGetLastError(), "launch dedispersion kernel");
+  return DD_OK;
+}
+
+dd_status dd_plan_run_stats(dd_plan *p, const void *d_input, float *d_output,
+                            dd_dm_accum *d_accum, void *stream) {
+  if (!p || !d_accum) return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (p->mode != DD_SINGLE_STEP || p->bits > 16)
+    return fail(DD_ERR_UNSUPPORTED,
+                "detection statistics are computed for single-step input of 1-16 bits");
+  dd::ProblemDesc P{};
+  dd_status st = dd::plan_problem(p, d_input, d_output, &P, nullptr);
+  if (st) return st;
+  const uint64_t tiles = (uint64_t)p->nr_groups * p->tiles_d * p->tiles_t;
+  const uint64_t rows = (uint64_t)p->nr_groups * p->dims.nr_dms;
+  DeviceGuard g(p->device);
+  if (!g.ok) return fail(DD_ERR_CUDA, "cannot select device %d", p->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  DD_CUDA(cudaMemsetAsync(d_accum, 0, rows * sizeof(dd_dm_accum), s), "clear statistics");
+  if (tiles == 0) return DD_OK;
+  const bool fused = p->kinfo->family == dd::kFamilyShared8;
+  if (fused) P.accum = reinterpret_cast<unsigned long long *>(d_accum);
+  p->kinfo->launch(P, (unsigned)tiles, p->smem, s);
+  DD_CUDA(cudaGetLastError(), "launch dedispersion kernel");
+  if (!fused)
+    DD_CUDA(dd::launch_row_stats(P, reinterpret_cast<unsigned long long *>(d_accum),
+                                 (uint32_t)rows, s),
+            "launch statistics kernel");
   return DD_OK;
 }
 

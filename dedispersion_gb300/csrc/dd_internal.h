@@ -101,6 +101,10 @@ struct ProblemDesc {
   uint32_t psw;                 // words per copy of one partial-sum series
   uint32_t slots;               // partial-sum series slots per stage
   uint32_t table_bytes;         // largest stage table (multiple of 16)
+  // Detection statistics of the output rows (NULL: not requested): per row
+  // {sum, sum of squares, peak << 32 | (0xffffffff - sample)}, accumulated
+  // with atomics by the shared-partial-sum kernel.
+  unsigned long long *accum;
 };
 
 // One entry of the kernel registry: a compiled tile configuration.

@@ -391,6 +391,41 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
       }
     }
   }
+  if (P.accum) {
+    // Detection statistics from the totals still in registers: a warp holds
+    // every sample of its DMs in this tile; one set of atomics per DM.
+#pragma unroll
+    for (int j = 0; j < ND; ++j) {
+      const uint32_t d = dtile * kTileD + ty * ND + j;
+      if (d >= P.nr_dms) continue;  // uniform over the warp
+      unsigned long long s1 = 0, s2 = 0, best = 0;
+#pragma unroll
+      for (int i = 0; i < NW; ++i)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const uint32_t t = t0 + 2u * (tx + 32u * i) + h, v = tot[j][i][h];
+          if (t < P.nr_samples) {
+            s1 += v;
+            s2 += (unsigned long long)v * v;
+            const unsigned long long key = ((unsigned long long)v << 32) | (0xFFFFFFFFu - t);
+            best = key > best ? key : best;
+          }
+        }
+#pragma unroll
+      for (int o = 16; o; o >>= 1) {
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+        const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, o);
+        best = ob > best ? ob : best;
+      }
+      if (tx == 0) {
+        unsigned long long *a = P.accum + 3ull * ((uint64_t)g_index * P.nr_dms + d);
+        atomicAdd(a, s1);
+        atomicAdd(a + 1, s2);
+        atomicMax(a + 2, best);
+      }
+    }
+  }
   return true;
 }
 

@@ -282,6 +282,36 @@ dd_status dd_plan_get_conf(const dd_plan *plan, dd_conf *conf);
 dd_status dd_plan_adds(const dd_plan *plan, uint64_t *adds);
 dd_status dd_plan_destroy(dd_plan *plan);
 
+/* ---- detection statistics of the output, computed in the same pass ------ */
+/* No counterpart in the reference: its output goes to the next program of a
+ * pipeline (an S/N search per DM), which reads the DM-time plane back from
+ * memory.  For single-step plans on input of 1-16 bits (integer sums), per
+ * output row (synthesized beam x DM): the exact sum and sum of squares of its
+ * samples and its largest sample, the earliest on ties.  The
+ * shared-partial-sum kernel accumulates them from its registers while it
+ * writes the row; the other kernels take one extra pass over the output. */
+typedef struct dd_dm_accum {
+  uint64_t sum;     /* sum of the row's samples */
+  uint64_t sum_sq;  /* sum of their squares */
+  uint64_t peak;    /* largest sample << 32 | (0xffffffff - its sample index) */
+} dd_dm_accum;
+typedef struct dd_dm_stats {
+  double mean;
+  double stddev;         /* population standard deviation */
+  double snr;            /* (peak - mean) / stddev; 0 when stddev is 0 */
+  float peak;
+  uint32_t peak_sample;
+} dd_dm_stats;
+/* dd_plan_run, and d_accum[beams x DMs] (device array, row = synthesized beam
+ * * nr_dms + DM) set to the statistics of the output it writes.  The call
+ * clears d_accum on `stream` first. */
+dd_status dd_plan_run_stats(dd_plan *plan, const void *d_input, float *d_output,
+                            dd_dm_accum *d_accum, void *stream);
+/* Host: mean, standard deviation, peak, its sample and S/N of `rows` rows of
+ * `samples` samples from their accumulators. */
+dd_status dd_dm_stats_from_accum(const dd_dm_accum *accum, size_t rows, uint32_t samples,
+                                 dd_dm_stats *stats);
+
 /* ---- batches: many beams in one persistent launch ------------------------ */
 /* No counterpart in the reference (its driver launches one kernel per beam
  * set, src/DedispersionTest.cpp:366-399).  A batch holds single-step problems
