@@ -198,6 +198,39 @@ def dd_out_row(obs):
     return dd.pad(obs.getNrSamplesPerBatch(), PADDING // 4)
 
 
+def bench_detect(torch, plan, d_in, d_out, stream, D, S, steps):
+    """The same launches with per-DM detection statistics (sum, sum of squares,
+    peak) accumulated in the same pass; reports its cost over the plain run and
+    the best S/N row of the last step."""
+    import dedispersion_gb300 as dd
+    d_acc = torch.empty((D, 3), dtype=torch.int64, device=d_out.device)
+    n = max(3, min(steps, 20))
+    for i in range(3):
+        plan.run_stats(d_in[i % len(d_in)], d_out, d_acc, stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e2 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for i in range(n):
+        plan.run(d_in[i % len(d_in)], d_out, stream)
+    e1.record(stream)
+    for i in range(n):
+        plan.run_stats(d_in[i % len(d_in)], d_out, d_acc, stream)
+    e2.record(stream)
+    plan.check(stream)
+    plain_ms, stats_ms = e0.elapsed_time(e1) / n, e1.elapsed_time(e2) / n
+    st = dd.dm_stats(d_acc.cpu().numpy().view(np.uint64), S)
+    best = int(np.argmax(st["snr"]))
+    return {"ms_per_step": stats_ms, "plain_ms_per_step": plain_ms,
+            "overhead": stats_ms / plain_ms - 1.0,
+            "fused_in_kernel": plan.conf().getNrItemsD2() == 8,
+            "best_row": {"dm_index": best, "snr": float(st["snr"][best]),
+                         "peak_sample": int(st["peak_sample"][best])},
+            "what": "per-DM sum, sum of squares and earliest peak of the output, exact "
+                    "integers, accumulated while dedispersing (dd_plan_run_stats)"}
+
+
 def bench_batched(torch, device: int, reps: int = 3, count: int = 40):
     """40 uneven beams (384/1536 ch, 8192-32768 samples, 512-4096 DMs, steps
     0.1-0.5, 2/4/8-bit uniform input) in one persistent launch replayed from a
@@ -427,6 +460,7 @@ def main():
     t_e2e = max_over_ranks(time.perf_counter() - t, pg, f"cuda:{local}")
     e2e_value = job_value(world, e2e_steps, D, S, t_e2e)
 
+    detect = bench_detect(torch, plan, d_in, d_out, stream, D, S, args.steps)
     batched = bench_batched(torch, local) if not args.no_batched else None
     served = bench_served(local) if not args.no_served else None
 
@@ -486,6 +520,7 @@ def main():
                                    f"channels), {cpu_dt:.2f} s wall on {cpu_threads} threads"},
         "clocks": clocks,
         "gpu_launches": args.steps * plan.launches(),
+        "detect": detect,
         "batched": batched,
         "served": served,
     }
