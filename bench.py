@@ -231,6 +231,44 @@ def bench_detect(torch, plan, d_in, d_out, stream, D, S, steps):
                     "integers, accumulated while dedispersing (dd_plan_run_stats)"}
 
 
+def bench_ingest(torch, inp, lay, obs, stream):
+    """Filterbank samples arrive time-major ([sample][channel]); the device
+    transpose puts this workload's whole input (29568 samples x 1536
+    channels, 45 MB) into channel rows.  Bytes moved = read + write."""
+    import ctypes as C
+    from dedispersion_gb300._abi import check, lib
+    S_disp, nch = obs.getNrSamplesPerDispersedBatch(), obs.getNrChannels()
+    rows = inp.reshape(nch, lay.input_row_bytes)[:, :S_disp]
+    d_src = torch.from_numpy(np.ascontiguousarray(rows[::-1].T)).cuda()
+    d_dst = torch.zeros(lay.input_bytes, dtype=torch.uint8, device=d_src.device)
+    n = 20
+
+    def once():
+        check(lib().dd_transpose_time_major(C.c_void_p(d_src.data_ptr()), S_disp, nch, 1,
+                                            C.c_void_p(d_dst.data_ptr()), lay.input_row_bytes,
+                                            0, C.c_void_p(stream.cuda_stream)))
+    for _ in range(3):
+        once()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(n):
+        once()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / n
+    exact = bool(np.array_equal(d_dst.cpu().numpy().reshape(nch, -1)[:, :S_disp], rows))
+    moved = 2 * S_disp * nch
+    try:
+        peak = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"]
+    except Exception:
+        peak = 6784.2
+    return {"ms": ms, "gbs": moved / ms / 1e6, "hbm_frac": moved / ms / 1e6 / peak,
+            "bytes": moved, "exact": exact,
+            "what": "time-major filterbank block -> channel rows (dd_transpose_time_major), "
+                    "descending-frequency file order reversed on the way"}
+
+
 def bench_batched(torch, device: int, reps: int = 3, count: int = 40):
     """40 uneven beams (384/1536 ch, 8192-32768 samples, 512-4096 DMs, steps
     0.1-0.5, 2/4/8-bit uniform input) in one persistent launch replayed from a
@@ -461,6 +499,7 @@ def main():
     e2e_value = job_value(world, e2e_steps, D, S, t_e2e)
 
     detect = bench_detect(torch, plan, d_in, d_out, stream, D, S, args.steps)
+    ingest_line = bench_ingest(torch, inp, lay, obs, stream)
     batched = bench_batched(torch, local) if not args.no_batched else None
     served = bench_served(local) if not args.no_served else None
 
@@ -521,6 +560,7 @@ def main():
         "clocks": clocks,
         "gpu_launches": args.steps * plan.launches(),
         "detect": detect,
+        "ingest": ingest_line,
         "batched": batched,
         "served": served,
     }

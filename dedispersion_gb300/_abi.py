@@ -124,6 +124,11 @@ SIGNATURES = {
     "dd_plan_launches": (C.c_int, [_P, _U32P]),
     "dd_plan_get_conf": (C.c_int, [_P, _CONF]),
     "dd_plan_adds": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    "dd_filterbank_info_read": (C.c_int, [C.c_char_p, _P]),
+    "dd_filterbank_read": (C.c_int, [C.c_char_p, _P, C.c_uint64, C.c_uint64, _P]),
+    "dd_filterbank_observation": (C.c_int, [_P, _P]),
+    "dd_transpose_time_major": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_int, _P, C.c_uint64,
+                                          C.c_uint64, _P]),
     "dd_plan_run_stats": (C.c_int, [_P, _P, _P, _P, _P]),
     "dd_dm_stats_from_accum": (C.c_int, [_P, C.c_size_t, C.c_uint32, _P]),
     "dd_plan_destroy": (C.c_int, [_P]),

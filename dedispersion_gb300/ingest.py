@@ -1,0 +1,93 @@
+"""SIGPROC filterbank input (the role of AstroData's readers in the reference).
+
+    fb = Filterbank("beam.fil")
+    fb.observation(obs)                 # channels, frequencies, sampling time
+    block = fb.read(start, count)       # [count][nchans] uint8, time-major
+    fb.to_rows(d_block, d_input, row_bytes, offset)   # device transpose
+
+The header is parsed and the samples are read by the library
+(``dd_filterbank_info_read``, ``dd_filterbank_read``); ``to_rows`` transposes
+a time-major device block into a plan's channel rows on the GPU, reversing
+the channel order for files whose frequencies descend (``foff < 0``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._abi import check, lib
+from . import Observation
+
+
+class FilterbankInfo(C.Structure):
+    _fields_ = [("nchans", C.c_uint32), ("nbits", C.c_uint32), ("nifs", C.c_uint32),
+                ("nbeams", C.c_uint32), ("ibeam", C.c_uint32), ("data_type", C.c_uint32),
+                ("nsamples", C.c_uint64), ("header_bytes", C.c_uint64), ("tsamp", C.c_double),
+                ("fch1", C.c_double), ("foff", C.c_double), ("tstart", C.c_double),
+                ("refdm", C.c_double), ("source_name", C.c_char * 80)]
+
+
+class Filterbank:
+    def __init__(self, path: str) -> None:
+        self.path = str(path)
+        self.info = FilterbankInfo()
+        check(lib().dd_filterbank_info_read(self.path.encode(), C.byref(self.info)))
+
+    @property
+    def reversed(self) -> bool:
+        """File channel 0 is the highest frequency (rows are filled reversed)."""
+        return self.info.foff < 0
+
+    def observation(self, obs: Observation) -> Observation:
+        """Set obs's channels, lowest frequency, bandwidth and sampling time."""
+        check(lib().dd_filterbank_observation(C.byref(self.info), C.byref(obs.c)))
+        return obs
+
+    def read(self, start: int, count: int) -> np.ndarray:
+        """Samples [start, start + count) of IF 0, time-major ([count][nchans]
+        for 8-bit files; raw bytes otherwise)."""
+        nbytes = count * self.info.nchans * self.info.nbits // 8
+        buf = np.empty(nbytes, dtype=np.uint8)
+        check(lib().dd_filterbank_read(self.path.encode(), C.byref(self.info), int(start),
+                                       int(count), buf.ctypes.data_as(C.c_void_p)))
+        if self.info.nbits == 8:
+            return buf.reshape(count, self.info.nchans)
+        return buf
+
+    def to_rows(self, d_block, d_rows, row_bytes: int, offset: int = 0, stream=None) -> None:
+        """Device: time-major 8-bit block -> channel rows at sample ``offset``."""
+        from . import _devptr, _stream
+        if self.info.nbits != 8:
+            raise ValueError("the device transpose takes 8-bit samples")
+        count = int(d_block.numel()) // self.info.nchans if hasattr(d_block, "numel") else None
+        if count is None:
+            raise TypeError("d_block must be a device tensor")
+        check(lib().dd_transpose_time_major(C.c_void_p(_devptr(d_block)), count,
+                                            self.info.nchans, 1 if self.reversed else 0,
+                                            C.c_void_p(_devptr(d_rows)), int(row_bytes),
+                                            int(offset), C.c_void_p(_stream(stream))))
+
+
+def write_filterbank(path: str, data: np.ndarray, *, fch1: float, foff: float, tsamp: float,
+                     tstart: float = 60000.0, source_name: str = "synthetic") -> None:
+    """Write a SIGPROC filterbank file: data is time-major [samples][nchans]
+    uint8 (file channel order).  For tests and examples."""
+    def s(x: str) -> bytes:
+        b = x.encode()
+        return np.int32(len(b)).tobytes() + b
+
+    def i(k: str, v: int) -> bytes:
+        return s(k) + np.int32(v).tobytes()
+
+    def d(k: str, v: float) -> bytes:
+        return s(k) + np.float64(v).tobytes()
+
+    data = np.ascontiguousarray(data, dtype=np.uint8)
+    hdr = (s("HEADER_START") + i("telescope_id", 0) + i("machine_id", 0) + i("data_type", 1)
+           + s("source_name") + s(source_name) + d("fch1", fch1) + d("foff", foff)
+           + i("nchans", data.shape[1]) + i("nbits", 8) + d("tstart", tstart) + d("tsamp", tsamp)
+           + i("nifs", 1) + s("HEADER_END"))
+    with open(path, "wb") as f:
+        f.write(hdr)
+        f.write(data.tobytes())

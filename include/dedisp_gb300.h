@@ -312,6 +312,38 @@ dd_status dd_plan_run_stats(dd_plan *plan, const void *d_input, float *d_output,
 dd_status dd_dm_stats_from_accum(const dd_dm_accum *accum, size_t rows, uint32_t samples,
                                  dd_dm_stats *stats);
 
+/* ---- ingest: SIGPROC filterbank files ------------------------------------ */
+/* The reference reads its input through AstroData's readers (ReadData, an
+ * external dependency, CMakeLists.txt:8-15); this is the SIGPROC filterbank
+ * path of that role, with the time-major to channel-row transpose on the
+ * device. */
+typedef struct dd_filterbank_info {
+  uint32_t nchans, nbits, nifs, nbeams, ibeam, data_type;
+  uint64_t nsamples;      /* from the header, else from the file size */
+  uint64_t header_bytes;  /* offset of the first sample */
+  double tsamp;           /* seconds */
+  double fch1, foff;      /* MHz: first channel, channel step (< 0: descending) */
+  double tstart, refdm;
+  char source_name[80];
+} dd_filterbank_info;
+/* Parse the header of a SIGPROC filterbank file. */
+dd_status dd_filterbank_info_read(const char *path, dd_filterbank_info *info);
+/* Samples [start, start + count) of IF 0, time-major, into a host buffer of
+ * count * nchans * nbits / 8 bytes. */
+dd_status dd_filterbank_read(const char *path, const dd_filterbank_info *info,
+                             uint64_t start, uint64_t count, void *time_major);
+/* Channel count, lowest frequency, bandwidth and sampling time of `obs`
+ * from the header: the engine's channel c is at min_freq + c * bandwidth, so
+ * files with foff < 0 are read with their channels reversed. */
+dd_status dd_filterbank_observation(const dd_filterbank_info *info, dd_observation *obs);
+/* Device: a time-major 8-bit block [count][nchans] into channel rows of a
+ * plan's input (row c at d_dst + c * dst_row_bytes), at sample
+ * dst_sample_offset of each row; `reverse` = 1 writes file channel c to row
+ * nchans - 1 - c.  Asynchronous on `stream`. */
+dd_status dd_transpose_time_major(const void *d_src, uint32_t count, uint32_t nchans,
+                                  int reverse, void *d_dst, uint64_t dst_row_bytes,
+                                  uint64_t dst_sample_offset, void *stream);
+
 /* ---- batches: many beams in one persistent launch ------------------------ */
 /* No counterpart in the reference (its driver launches one kernel per beam
  * set, src/DedispersionTest.cpp:366-399).  A batch holds single-step problems
