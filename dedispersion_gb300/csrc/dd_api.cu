@@ -582,6 +582,16 @@ int plan_family(const dd_plan *p) {
   return p->kinfo->family;
 }
 
+// Launches `p`'s kernel over all its tiles with arguments `P` (from
+// plan_problem, possibly with another status word) on `stream`.
+dd_status plan_launch(const dd_plan *p, const ProblemDesc &P, cudaStream_t stream) {
+  const uint64_t tiles = (uint64_t)p->nr_groups * p->tiles_d * p->tiles_t;
+  if (tiles == 0) return DD_OK;
+  p->kinfo->launch(P, (unsigned)tiles, p->smem, stream);
+  DD_CUDA(cudaGetLastError(), "launch dedispersion kernel");
+  return DD_OK;
+}
+
 // The kernel arguments of one run of `p` on the given device buffers; also
 // the rows each group sums (the cost of one of its tiles).
 dd_status plan_problem(const dd_plan *p, const void *d_input, float *d_output,

@@ -344,13 +344,16 @@ dd_status dd_transpose_time_major(const void *d_src, uint32_t count, uint32_t nc
                                   int reverse, void *d_dst, uint64_t dst_row_bytes,
                                   uint64_t dst_sample_offset, void *stream);
 
-/* ---- batches: many beams in one persistent launch ------------------------ */
+/* ---- batches: many beams in one graph launch ----------------------------- */
 /* No counterpart in the reference (its driver launches one kernel per beam
  * set, src/DedispersionTest.cpp:366-399).  A batch holds single-step problems
  * of 1/2/4/8-bit input, each with its own geometry, tables and device
- * buffers; committing it builds one work list over all their tiles (longest
- * first) and records a CUDA graph of [reset work counter, persistent kernel].
- * Results equal dd_plan_run's for each problem bit for bit. */
+ * buffers; committing it records one CUDA graph that computes them all.  When
+ * every problem fits the shared-partial-sum tile the graph forks into a few
+ * concurrent branches of the problems' own kernels (longest first, balanced
+ * by tile cost); otherwise it is one work list over all the problems' tiles
+ * (longest first) run by a persistent direct-tile kernel.  Results equal
+ * dd_plan_run's for each problem bit for bit. */
 typedef struct dd_batch dd_batch;
 dd_status dd_batch_create(dd_batch **batch, int device);
 /* Add one single-step problem; `index` (may be NULL) receives its position.
@@ -366,7 +369,8 @@ dd_status dd_batch_commit(dd_batch *batch);
 dd_status dd_batch_run(dd_batch *batch, void *stream, int use_graph);
 /* Synchronize `stream` and report a device-side timeout. */
 dd_status dd_batch_check(dd_batch *batch, void *stream);
-/* Problems, tiles and persistent CTAs of a committed batch. */
+/* Problems and tiles of a committed batch, and its persistent CTAs (direct
+ * tile) or concurrent branches (shared tile). */
 dd_status dd_batch_info(const dd_batch *batch, uint32_t *problems,
                         uint32_t *tiles, uint32_t *grid);
 /* 1 if a committed batch runs the shared-partial-sum tile (every problem's

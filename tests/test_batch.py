@@ -1,6 +1,8 @@
-"""Batched persistent launch: uneven beams of mixed input widths in one
-launch (replayed from a CUDA graph) give, beam by beam, exactly the plain
-path's output; one beam is also checked against the CPU oracle."""
+"""Batches: uneven beams of mixed input widths in one CUDA graph launch give,
+beam by beam, exactly the plain path's output, both in the shared-tile form
+(the beams' own kernels on concurrent branches) and in the direct-tile form
+(one persistent kernel, taken when a beam does not fit the shared tile); one
+beam is also checked against the CPU oracle."""
 import numpy as np
 import pytest
 
@@ -18,10 +20,10 @@ SHAPES = [
 ]
 
 
-def build(torch, padding=64):
+def build(torch, padding=64, shapes=SHAPES):
     beams = []
-    for sh in SHAPES:
-        obs = syn.shape_observation(sh, padding)
+    for sh in shapes:
+        obs = sh["obs"] if "obs" in sh else syn.shape_observation(sh, padding)
         shifts = dd.getShifts(obs, padding)
         zapped = syn.zapped_mask(sh["channels"], 0.1, sh["seed"], padding)
         mapping = syn.identity_mapping(obs, padding)
@@ -32,16 +34,8 @@ def build(torch, padding=64):
     return beams
 
 
-def test_batch_matches_plain_path(gpu, oracle):
+def _equals_plain(batch, beams, padding):
     torch = pytest.importorskip("torch")
-    padding = 64
-    beams = build(torch, padding)
-    batch = dd.Batch()
-    for sh, obs, shifts, zapped, mapping, d_in, d_out, lay in beams:
-        batch.add(obs, sh["bits"], padding, shifts, zapped, mapping, d_in, d_out)
-    batch.commit()
-    info = batch.info()
-    assert info["problems"] == len(SHAPES) and info["tiles"] > 0 and info["grid"] > 0
     for graph in (True, True, False):  # two graph replays, then a direct launch
         for b in beams:
             b[6].fill_(-1.0)
@@ -61,6 +55,20 @@ def test_batch_matches_plain_path(gpu, oracle):
             g = d_out.view(rows, -1)[:, :S]
             w = want.view(rows, -1)[:, :S]
             assert torch.equal(g, w), sh
+
+
+def test_batch_matches_plain_path(gpu, oracle):
+    torch = pytest.importorskip("torch")
+    padding = 64
+    beams = build(torch, padding)
+    batch = dd.Batch()
+    for sh, obs, shifts, zapped, mapping, d_in, d_out, lay in beams:
+        batch.add(obs, sh["bits"], padding, shifts, zapped, mapping, d_in, d_out)
+    batch.commit()
+    info = batch.info()
+    assert info["problems"] == len(SHAPES) and info["tiles"] > 0
+    assert info["tile"] == "shared" and 1 <= info["grid"] <= len(SHAPES)
+    _equals_plain(batch, beams, padding)
     # one beam against the CPU oracle
     sh, obs, shifts, zapped, mapping, d_in, d_out, lay = beams[1]
     ref = np.zeros(lay.output_bytes // 4, np.float32)
@@ -69,4 +77,22 @@ def test_batch_matches_plain_path(gpu, oracle):
     S = obs.getNrSamplesPerBatch()
     got = d_out.cpu().numpy().reshape(-1, lay.output_row_elems)[:, :S]
     np.testing.assert_array_equal(got, ref.reshape(-1, lay.output_row_elems)[:, :S])
+    batch.close()
+
+
+def test_batch_direct_tile_when_a_beam_does_not_fit(gpu):
+    """A beam whose delays spread too far for the shared tile (300 MHz, DM
+    step 8) moves the whole batch to the persistent direct-tile kernel."""
+    torch = pytest.importorskip("torch")
+    padding = 64
+    wide = dict(obs=syn.make_observation(128, 300.0, 1.0, 81.92e-6, 512, 64, 0.0, 8.0,
+                                         padding=padding), channels=128, bits=8, seed=9)
+    beams = build(torch, padding, SHAPES[:3] + [wide])
+    batch = dd.Batch()
+    for sh, obs, shifts, zapped, mapping, d_in, d_out, lay in beams:
+        batch.add(obs, sh["bits"], padding, shifts, zapped, mapping, d_in, d_out)
+    batch.commit()
+    info = batch.info()
+    assert info["tile"] == "direct" and info["grid"] > 0 and info["problems"] == 4
+    _equals_plain(batch, beams, padding)
     batch.close()
