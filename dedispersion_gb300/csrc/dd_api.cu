@@ -414,6 +414,15 @@ dd_status rebuild(dd_plan *p) {
                                                     d.nr_dms, p->bits, budget, &p->shared);
     if (!why.empty()) return fail(DD_ERR_UNSUPPORTED, "tile %s: %s", k.name, why.c_str());
   }
+  const uint32_t bits = family_bits(p->mode, p->bits) == 8 ? p->bits : family_bits(p->mode, p->bits);
+  const uint32_t a = dd::window_alignment_samples(bits);
+  p->win = shared ? 0 : ((k.tile_t + spread + a + 8) + 15) / 16 * 16;
+  p->smem = shared ? p->shared.smem : dd::kernel_smem_bytes(k, p->win, bits);
+  if (p->smem > (size_t)dev_max)
+    return fail(DD_ERR_UNSUPPORTED,
+                "tile %s needs %zu bytes of shared memory (window %u samples), device allows %d; "
+                "use a configuration with fewer DMs per tile",
+                k.name, p->smem, p->win, dev_max);
   // Delay table: the offsets of each DM tile's delays from the delay of its
   // first DM, per delay row (the same float order as the device's
   // dev_delay).  16-bit offsets: skipped if a spread does not fit.
@@ -441,15 +450,6 @@ dd_status rebuild(dd_plan *p) {
       }
     }
   }
-  const uint32_t bits = family_bits(p->mode, p->bits) == 8 ? p->bits : family_bits(p->mode, p->bits);
-  const uint32_t a = dd::window_alignment_samples(bits);
-  p->win = shared ? 0 : ((k.tile_t + spread + a + 8) + 15) / 16 * 16;
-  p->smem = shared ? p->shared.smem : dd::kernel_smem_bytes(k, p->win, bits);
-  if (p->smem > (size_t)dev_max)
-    return fail(DD_ERR_UNSUPPORTED,
-                "tile %s needs %zu bytes of shared memory (window %u samples), device allows %d; "
-                "use a configuration with fewer DMs per tile",
-                k.name, p->smem, p->win, dev_max);
   // Upload.
   DeviceGuard g(p->device);
   if (p->groups.size() > p->cap_groups) {
@@ -535,14 +535,37 @@ dd_status rebuild(dd_plan *p) {
 
 // rebuild(), and for plans created without a configuration: the default
 // shared kernel, else (a shape it cannot take) the default direct kernel.
+// A plan without a configuration runs the default kernel of its shape; where
+// that tile does not fit (its tables or window outgrow shared memory) the
+// direct default, then the other direct tiles of the same width, largest
+// (samples x DMs x rows per stage) first.
 dd_status rebuild_auto(dd_plan *p) {
   if (p->auto_kernel) p->kinfo = default_kernel(p->mode, p->bits, true);
   dd_status st = rebuild(p);
-  if (st == DD_ERR_UNSUPPORTED && p->auto_kernel && p->kinfo->family == dd::kFamilyShared8) {
-    p->kinfo = default_kernel(p->mode, p->bits, false);
+  if (st != DD_ERR_UNSUPPORTED || !p->auto_kernel) return st;
+  const std::string first = g_error;
+  const dd::KernelInfo *direct = default_kernel(p->mode, p->bits, false);
+  std::vector<const dd::KernelInfo *> cands;
+  if (p->kinfo != direct) cands.push_back(direct);
+  int n = 0;
+  const dd::KernelInfo *reg = dd::kernel_registry(&n);
+  std::vector<const dd::KernelInfo *> rest;
+  for (int i = 0; i < n; i++)
+    if (&reg[i] != direct && reg[i].family == direct->family &&
+        reg[i].elem_bits == direct->elem_bits)
+      rest.push_back(&reg[i]);
+  std::stable_sort(rest.begin(), rest.end(), [](const dd::KernelInfo *x, const dd::KernelInfo *y) {
+    return (uint64_t)x->tile_t * x->tile_d * x->channels >
+           (uint64_t)y->tile_t * y->tile_d * y->channels;
+  });
+  cands.insert(cands.end(), rest.begin(), rest.end());
+  for (const dd::KernelInfo *k : cands) {
+    p->kinfo = k;
     st = rebuild(p);
+    if (st != DD_ERR_UNSUPPORTED) return st;
   }
-  return st;
+  p->kinfo = default_kernel(p->mode, p->bits, true);
+  return fail(DD_ERR_UNSUPPORTED, "no tile fits this shape: %s", first.c_str());
 }
 
 }  // namespace

@@ -80,12 +80,14 @@ def test_batch_matches_plain_path(gpu, oracle):
     batch.close()
 
 
-def test_batch_direct_tile_when_a_beam_does_not_fit(gpu):
-    """A beam whose delays spread too far for the shared tile (300 MHz, DM
-    step 8) moves the whole batch to the persistent direct-tile kernel."""
+def test_batch_direct_tile_when_a_beam_does_not_fit(gpu, oracle):
+    """A beam whose partial sums do not fit the shared tile (1 MHz channels
+    from 300 MHz, DM step 0.12: ~34 samples more delay per DM step in the
+    lowest channel) moves the whole batch to the persistent direct-tile
+    kernel."""
     torch = pytest.importorskip("torch")
     padding = 64
-    wide = dict(obs=syn.make_observation(128, 300.0, 1.0, 81.92e-6, 512, 64, 0.0, 8.0,
+    wide = dict(obs=syn.make_observation(128, 300.0, 1.0, 81.92e-6, 512, 64, 0.0, 0.12,
                                          padding=padding), channels=128, bits=8, seed=9)
     beams = build(torch, padding, SHAPES[:3] + [wide])
     batch = dd.Batch()
@@ -95,4 +97,11 @@ def test_batch_direct_tile_when_a_beam_does_not_fit(gpu):
     info = batch.info()
     assert info["tile"] == "direct" and info["grid"] > 0 and info["problems"] == 4
     _equals_plain(batch, beams, padding)
+    # the wide beam (a default plan falls back to a smaller direct tile) against the oracle
+    sh, obs, shifts, zapped, mapping, d_in, d_out, lay = beams[3]
+    ref = np.zeros(lay.output_bytes // 4, np.float32)
+    oracle.dedispersion(obs.c, zapped, mapping, d_in.cpu().numpy(), ref, shifts, padding, 8)
+    S = obs.getNrSamplesPerBatch()
+    got = d_out.cpu().numpy().reshape(-1, lay.output_row_elems)[:, :S]
+    np.testing.assert_array_equal(got, ref.reshape(-1, lay.output_row_elems)[:, :S])
     batch.close()
