@@ -319,6 +319,88 @@ def subbandDedispersionStepTwo(observation: Observation, beamMapping, input: np.
                                                  _ptr(sh, C.c_float), padding))
 
 
+def subbandDedispersion(observation: Observation, zappedChannels, beamMapping, input: np.ndarray,
+                        output: np.ndarray, shifts, shiftsStepTwo, padding: int,
+                        inputBits: int) -> None:
+    """subbandDedispersionStepOne followed by subbandDedispersionStepTwo
+    (include/Dedispersion.hpp:60-61) in one call, the intermediate kept on the
+    device (packed 16-bit sums where they fit); input in step one's layout,
+    output in step two's, equal to the two calls bit for bit."""
+    inp = np.ascontiguousarray(input)
+    l1 = layout(observation, DD_STEP_ONE, inputBits, padding)
+    l2 = layout(observation, DD_STEP_TWO, 32, padding)
+    _check_buffers(inp, output, DdLayout(input_row_bytes=l1.input_row_bytes,
+                                         input_bytes=l1.input_bytes,
+                                         output_row_elems=l2.output_row_elems,
+                                         output_bytes=l2.output_bytes))
+    z, m = _u32(zappedChannels), _u32(beamMapping)
+    sh = np.ascontiguousarray(shifts, dtype=np.float32)
+    sh2 = np.ascontiguousarray(shiftsStepTwo, dtype=np.float32)
+    check(lib().dd_subband_dedispersion(C.byref(observation.c), _ptr(z, C.c_uint32),
+                                        _ptr(m, C.c_uint32), _ptr(inp), _ptr(output, C.c_float),
+                                        _ptr(sh, C.c_float), _ptr(sh2, C.c_float), padding,
+                                        inputBits))
+
+
+class SubbandPipeline:
+    """Device pipeline of the subband method (dd_subband_*): step one then
+    step two on device buffers, the intermediate owned by the pipeline."""
+
+    def __init__(self, observation: Observation, inputBits: int, padding: int, device: int = 0):
+        self.observation = observation.copy()
+        self.inputBits, self.padding = inputBits, padding
+        self._h = C.c_void_p()
+        check(lib().dd_subband_create(C.byref(self._h), C.byref(self.observation.c), inputBits,
+                                      padding, device))
+        self.layout_in = layout(self.observation, DD_STEP_ONE, inputBits, padding)
+        self.layout_out = layout(self.observation, DD_STEP_TWO, 32, padding)
+
+    def setTables(self, shifts, shiftsStepTwo, zapped, mapping) -> None:
+        sh = np.ascontiguousarray(shifts, dtype=np.float32)
+        sh2 = np.ascontiguousarray(shiftsStepTwo, dtype=np.float32)
+        z, m = _u32(zapped), _u32(mapping)
+        check(lib().dd_subband_set_tables(self._h, _ptr(sh, C.c_float), sh.size,
+                                          _ptr(sh2, C.c_float), sh2.size,
+                                          _ptr(z, C.c_uint32), z.size, _ptr(m, C.c_uint32),
+                                          m.size))
+
+    def setPairKernel(self, index: int) -> None:
+        check(lib().dd_subband_set_pair_kernel(self._h, int(index)))
+
+    def run(self, d_input, d_output, stream=None) -> None:
+        check(lib().dd_subband_run(self._h, C.c_void_p(_devptr(d_input)),
+                                   C.c_void_p(_devptr(d_output)), C.c_void_p(_stream(stream))))
+
+    def check(self, stream=None) -> None:
+        check(lib().dd_subband_check(self._h, C.c_void_p(_stream(stream))))
+
+    def info(self) -> dict:
+        packed, nbytes = C.c_int(0), C.c_uint64(0)
+        check(lib().dd_subband_info(self._h, C.byref(packed), C.byref(nbytes)))
+        return {"packed": bool(packed.value), "intermediate_bytes": nbytes.value}
+
+    def close(self) -> None:
+        if self._h:
+            lib().dd_subband_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self) -> None:
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self) -> "SubbandPipeline":
+        return self
+
+    def __exit__(self, *exc) -> None:
+        self.close()
+
+
+def pair_kernel_count() -> int:
+    return int(lib().dd_subband_pair_kernel_count())
+
+
 def readTunedDedispersionConf(filename: str, device: str, nrDMs: int) -> DedispersionConf:
     """The (device, nrDMs) entry of a tuned-configuration file
     (src/Dedispersion.cpp:20-81).  Raises DedispersionError(DD_ERR_FILE) if the

@@ -108,6 +108,17 @@ SIGNATURES = {
                                                    C.c_uint32, C.c_uint32]),
     "dd_subband_dedispersion_step_two": (C.c_int, [_OBS, _U32P, _F32P, _F32P, _F32P,
                                                    C.c_uint32]),
+    "dd_subband_create": (C.c_int, [C.POINTER(_P), _OBS, C.c_uint32, C.c_uint32, C.c_int]),
+    "dd_subband_set_tables": (C.c_int, [_P, _F32P, C.c_size_t, _F32P, C.c_size_t, _U32P,
+                                        C.c_size_t, _U32P, C.c_size_t]),
+    "dd_subband_run": (C.c_int, [_P, _P, _P, _P]),
+    "dd_subband_check": (C.c_int, [_P, _P]),
+    "dd_subband_info": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_uint64)]),
+    "dd_subband_set_pair_kernel": (C.c_int, [_P, C.c_int]),
+    "dd_subband_pair_kernel_count": (C.c_int, []),
+    "dd_subband_destroy": (C.c_int, [_P]),
+    "dd_subband_dedispersion": (C.c_int, [_OBS, _U32P, _U32P, _P, _F32P, _F32P, _F32P,
+                                          C.c_uint32, C.c_uint32]),
     "dd_dedispersion_noalloc": (C.c_int, [_OBS, _U32P, _U32P, _P, _F32P, _F32P, C.c_uint32,
                                           C.c_uint32, _P]),
     "dd_plan_create": (C.c_int, [C.POINTER(_P), _OBS, C.c_int, C.c_uint32, C.c_uint32,

@@ -194,10 +194,23 @@ const dd::KernelInfo *find_kernel(dd_mode mode, uint32_t bits, const dd_conf &c)
 // entry of its family; for single-step input of 1-8 bits the first
 // shared-partial-sum entry when `shared` (plans fall back to the direct
 // entry where a shape does not fit the shared tables).
+// Default tiles of the subband steps, where they differ from the first entry
+// of their input width (fastest of a sweep of every registry entry at 1536
+// channels, 32 subbands, 64 x 32 DMs, 24576 samples: step one's 64 coarse
+// DMs favour 8 DMs per thread, step two's 32 subband rows 8 x 8 items).
+const char *subband_default_name(dd_mode mode, uint32_t fb) {
+  if (mode == DD_STEP_ONE && fb == 8) return "swar8_i2_d8_w8_c16_vkUnpackPermuteMad";
+  if (mode == DD_STEP_TWO) return "scalar32_i8_d8_w4_c16";
+  return nullptr;
+}
+
 const dd::KernelInfo *default_kernel(dd_mode mode, uint32_t bits, bool shared) {
   int n = 0;
   const dd::KernelInfo *reg = dd::kernel_registry(&n);
   const uint32_t fb = family_bits(mode, bits);
+  if (const char *name = subband_default_name(mode, fb))
+    for (int i = 0; i < n; i++)
+      if (std::strcmp(reg[i].name, name) == 0) return &reg[i];
   const bool want_shared = shared && mode == DD_SINGLE_STEP && bits <= 8;
   for (int i = 0; i < n; i++)
     if ((uint32_t)reg[i].elem_bits == fb &&
@@ -284,6 +297,10 @@ struct dd_plan {
   // Tables changed since the last build: setters only record their table;
   // the first use (run, timing, queries) builds once.
   bool dirty = false;
+  // Packed subband intermediate (ProblemDesc::packed): step one writes it,
+  // step two (a pair tile) reads it; set by a subband pipeline only.
+  bool packed = false;
+  uint32_t flush_rows = 0;  // step two: rows per 16-bit lane flush
 };
 
 namespace {
@@ -323,6 +340,8 @@ dd_status rebuild(dd_plan *p) {
     }
   } else if (p->mode == DD_STEP_ONE) {
     const uint32_t SB = o->nr_subbands, cps = C / SB;
+    // Packed: rows (beam, coarse DM pair, subband) of 32-bit words.
+    const uint64_t dm_rows = p->packed ? (d.nr_dms + 1) / 2 : d.nr_dms;
     p->nr_groups = o->nr_beams * SB;
     p->out_dm_stride = (uint64_t)SB * d.out_row;
     std::vector<uint32_t> sb_row(SB);
@@ -338,7 +357,7 @@ dd_status rebuild(dd_plan *p) {
     for (uint32_t b = 0; b < o->nr_beams; b++)
       for (uint32_t sb = 0; sb < SB; sb++) {
         dd::GroupDesc G{(uint32_t)p->entries.size(), 0,
-                        ((uint64_t)b * d.nr_dms * SB + sb) * d.out_row};
+                        ((uint64_t)b * dm_rows * SB + sb) * d.out_row};
         uint32_t row = sb_row[sb];
         for (uint32_t c = sb * cps; c < (sb + 1) * cps; c++) {
           if (zapped(c)) continue;
@@ -350,20 +369,23 @@ dd_status rebuild(dd_plan *p) {
       }
   } else {
     const uint32_t SB = o->nr_subbands, D1 = o->nr_dms_subbanding;
-    p->nr_groups = o->nr_synthesized_beams * D1;
+    // Packed: one group per pair of coarse DMs, reading the pair's rows.
+    const uint32_t G1 = p->packed ? (D1 + 1) / 2 : D1;
+    p->nr_groups = o->nr_synthesized_beams * G1;
     p->out_dm_stride = d.out_row;
     for (uint32_t sb = 0; sb < SB; sb++) p->delay_shift.push_back(p->shifts[sb]);
     for (uint32_t g = 0; g < o->nr_synthesized_beams; g++)
-      for (uint32_t d1 = 0; d1 < D1; d1++) {
+      for (uint32_t d1 = 0; d1 < G1; d1++) {
+        const uint64_t first = p->packed ? 2ull * d1 : d1;  // coarse DM of the lanes' low half
         dd::GroupDesc G{(uint32_t)p->entries.size(), SB,
-                        ((uint64_t)g * D1 * d.nr_dms + (uint64_t)d1 * d.nr_dms) * d.out_row};
+                        ((uint64_t)g * D1 * d.nr_dms + first * d.nr_dms) * d.out_row};
         for (uint32_t s = 0; s < SB; s++) {
           uint64_t beam = p->mapping.empty() ? (o->nr_beams ? g % o->nr_beams : 0)
                                              : p->mapping[(uint64_t)g * d.mapping_row + s];
           if (beam >= o->nr_beams)
             return fail(DD_ERR_INVALID_ARGUMENT, "beam mapping[%u][%u] = %llu >= nr_beams %u",
                         g, s, (unsigned long long)beam, o->nr_beams);
-          p->entries.push_back({((beam * D1 + d1) * SB + s) * d.row_bytes, p->shifts[s], s});
+          p->entries.push_back({((beam * G1 + d1) * SB + s) * d.row_bytes, p->shifts[s], s});
         }
         p->groups.push_back(G);
       }
@@ -403,6 +425,26 @@ dd_status rebuild(dd_plan *p) {
                                    p->device), "query shared memory");
   }
   const bool shared = k.family == dd::kFamilyShared8;
+  if (p->packed && p->mode == DD_STEP_ONE) {
+    if (k.family != dd::kFamilySwar8 || k.items_d % 2)
+      return fail(DD_ERR_UNSUPPORTED, "a packed step one runs a swar8 tile (got %s)", k.name);
+    const uint32_t SB = o->nr_subbands, cps = C / SB;
+    uint32_t live_max = 0;
+    for (uint32_t sb = 0; sb < SB; sb++) {
+      uint32_t live = 0;
+      for (uint32_t c = sb * cps; c < (sb + 1) * cps; c++) live += zapped(c) ? 0u : 1u;
+      live_max = std::max(live_max, live);
+    }
+    if ((uint64_t)live_max * ((1u << p->bits) - 1u) > 0xFFFFu)
+      return fail(DD_ERR_UNSUPPORTED,
+                  "%u live channels of %u-bit input per subband can exceed 16-bit sums",
+                  live_max, p->bits);
+  } else if (p->packed && p->mode == DD_STEP_TWO) {
+    if (k.family != dd::kFamilyPair16 || p->flush_rows == 0)
+      return fail(DD_ERR_UNSUPPORTED, "a packed step two runs a pair tile");
+  } else if (k.family == dd::kFamilyPair16) {
+    return fail(DD_ERR_UNSUPPORTED, "pair tiles read a packed step-one intermediate only");
+  }
   if (shared) {
     if (p->mode != DD_SINGLE_STEP || p->bits > 8)
       return fail(DD_ERR_UNSUPPORTED, "kernel %s computes single-step 1/2/4/8-bit input only",
@@ -596,6 +638,28 @@ void set_last_error(const char *message) { g_error = message; }
 // Keep `bytes` of a block's shared memory free (before the tables are built).
 void plan_set_smem_reserve(dd_plan *p, uint32_t bytes) { p->smem_reserve = bytes; }
 
+// Makes `p` a stage of a subband pipeline with the packed intermediate: step
+// one writes pairs of coarse DMs; step two reads them with pair tile `k`,
+// widening lanes every `flush_rows` rows.  Before the tables are built.
+void plan_set_packed(dd_plan *p, const KernelInfo *k, uint32_t flush_rows) {
+  p->packed = true;
+  p->flush_rows = flush_rows;
+  if (k) p->kinfo = k;
+  p->auto_kernel = false;
+  p->dirty = true;
+  p->ready = false;
+}
+
+// Undoes plan_set_packed: float steps on the default kernel again.
+void plan_clear_packed(dd_plan *p) {
+  p->packed = false;
+  p->flush_rows = 0;
+  p->kinfo = default_kernel(p->mode, p->bits, true);
+  p->auto_kernel = true;
+  p->dirty = true;
+  p->ready = false;
+}
+
 // Whether the plan's tables are built (a deferred error leaves them unbuilt).
 bool plan_ready(const dd_plan *p) { return ensure_built(p) == DD_OK && p->ready; }
 
@@ -652,6 +716,14 @@ dd_status plan_problem(const dd_plan *p, const void *d_input, float *d_output,
   if (p->use_delay_tables) {
     P.delay_rows = (uint32_t)p->delay_shift.size();
     P.delay_rel = p->d_delay_rel;
+  }
+  if (p->packed) {
+    const uint32_t D1 = p->obs.nr_dms_subbanding;
+    P.packed = 1;
+    P.pair_groups = (D1 + 1) / 2;
+    P.pair_d1 = D1;
+    P.flush_rows = p->flush_rows;
+    P.pair_stride = (uint64_t)d.nr_dms * d.out_row;
   }
   if (p->kinfo->family == kFamilyShared8) {
     P.stage_rows = p->d_stage_rows;

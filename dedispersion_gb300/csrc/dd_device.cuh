@@ -12,7 +12,7 @@
 // the reference's local-memory kernel (include/Dedispersion.hpp:225-309),
 // which copies each channel's window into __local memory.
 //
-// Two tile families:
+// Three tile families:
 //
 // * swar8 (input of 1, 2, 4 or 8 bits).  Rows are expanded to one byte per
 //   sample while staged and kept as four copies shifted by 0..3 bytes, so a
@@ -26,6 +26,10 @@
 //   offset; 16-bit input accumulates in uint32, float input in float32 in row
 //   order, the reference's own order (include/Dedispersion.hpp:79-104), so
 //   float results are identical to the reference's.
+//
+// * pair (step two over the packed subband intermediate, ProblemDesc::
+//   packed).  A 32-bit word holds the 16-bit step-one sums of two coarse
+//   DMs; one load and one add serve both.
 //
 // Every wait on a bulk copy is bounded (kWaitNs); when one runs out the CTA
 // sets kStatusTimeout in the problem's status word, waits a bounded time for
@@ -536,6 +540,37 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
   sc += nst;
   flush();
 
+  if (P.packed) {
+    // Pairs (2p, 2p + 1) of the thread's DMs (d0 and NDT even): exact sums
+    // below 2^16, the host checked.
+    static_assert(NDT % 2 == 0, "DM pairs per thread");
+#pragma unroll
+    for (int j = 0; j < NDT; j += 2) {
+      const uint32_t d = d0 + ty * NDT + j;
+      if (d >= P.nr_dms) continue;
+      const bool hi_ok = d + 1u < P.nr_dms;
+      uint32_t *orow = reinterpret_cast<uint32_t *>(P.out) + G.out_offset +
+                       (uint64_t)(d >> 1) * P.out_dm_stride;
+#pragma unroll
+      for (int i = 0; i < NW; ++i) {
+        const uint32_t t = t0 + 4u * (tx + 32u * i);
+        uint32_t w[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          w[k] = t + k < P.nr_samples
+                     ? (tot[j][i][k] | (hi_ok ? tot[j + 1][i][k] << 16 : 0u)) : 0u;
+        if (P.out_vec4 && t + 3u < P.nr_samples) {
+          *reinterpret_cast<uint4 *>(orow + t) = make_uint4(w[0], w[1], w[2], w[3]);
+        } else {
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            if (t + k < P.nr_samples) orow[t + k] = w[k];
+        }
+      }
+    }
+    return true;
+  }
+
 #pragma unroll
   for (int j = 0; j < NDT; ++j) {
     const uint32_t d = d0 + ty * NDT + j;
@@ -682,6 +717,129 @@ __device__ __forceinline__ bool scalar_tile(const ProblemDesc &P,
     for (int i = 0; i < NS; ++i) {
       const uint32_t t = t0 + tx + 32u * i;
       if (t < P.nr_samples) orow[t] = (float)acc[j][i];
+    }
+  }
+  return true;
+}
+
+// ---- pair tile (step two over a packed intermediate) ----------------------
+
+// Step two of the subband method over the packed step-one rows (words of two
+// coarse DMs' 16-bit sums, ProblemDesc::packed): every 32-bit shared load
+// feeds one add of two 16-bit lanes, i.e. two of the reference's float adds
+// (include/Dedispersion.hpp:166-170), exact because the sums are integers.
+// Lanes widen into 32-bit totals every P.flush_rows rows, before they can
+// overflow.  Staging, delays and the pipeline are the scalar tile's.
+template <int NS, int NDT, int TY, int CH>
+__device__ __forceinline__ bool pair_tile(const ProblemDesc &P, uint32_t g,
+                                          const GroupDesc &G, uint32_t dtile,
+                                          uint32_t ttile, uint8_t *smem,
+                                          const SmemLayout &L, uint32_t &sc) {
+  constexpr int kTileT = 32 * NS;
+  constexpr int kTileD = TY * NDT;
+  constexpr int kThreads = 32 * TY;
+  constexpr int kAhead = kNRaw - 1;
+  static_assert(CH <= 32, "CH rows per stage <= 32");
+  const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+  const uint32_t t0 = ttile * kTileT, d0 = dtile * kTileD;
+  const uint32_t K = G.entry_count;
+  const uint32_t nst = (K + CH - 1) / CH;
+  StageCtx S;
+  S.bars = reinterpret_cast<uint64_t *>(smem + L.off_bar);
+  S.wstart = reinterpret_cast<uint32_t *>(smem + L.off_wstart);
+  S.wmod = S.wstart + kNRaw * CH;
+  S.raw = smem + L.off_raw;
+  S.raw_bytes = L.raw_bytes;
+  S.raw_stride = L.raw_stride;
+  uint32_t *table = reinterpret_cast<uint32_t *>(smem + L.off_table);
+  const uint32_t raws = smem_addr(S.raw) + 4u * tx;
+
+  if (ty == 0) {
+    const uint32_t pro = nst < (uint32_t)kAhead ? nst : (uint32_t)kAhead;
+    for (uint32_t s = 0; s < pro; ++s)
+      issue_stage<CH>(P, G, S, s, sc + s, t0, d0, dtile, tx);
+  }
+
+  uint32_t acc[NDT][NS], tlo[NDT][NS], thi[NDT][NS];
+#pragma unroll
+  for (int j = 0; j < NDT; ++j)
+#pragma unroll
+    for (int i = 0; i < NS; ++i) acc[j][i] = tlo[j][i] = thi[j][i] = 0;
+  auto widen = [&]() {
+#pragma unroll
+    for (int j = 0; j < NDT; ++j)
+#pragma unroll
+      for (int i = 0; i < NS; ++i) {
+        tlo[j][i] += acc[j][i] & 0xFFFFu;
+        thi[j][i] += acc[j][i] >> 16;
+        acc[j][i] = 0;
+      }
+  };
+  uint32_t since = 0;
+  using Delays = StageDelays<CH, kTileD, kThreads>;
+  Delays delays;
+  if (nst) delays.load(P, G, 0, dtile, K < (uint32_t)CH ? K : CH);
+
+  for (uint32_t s = 0; s < nst; ++s) {
+    const uint32_t gs = sc + s, slot = gs % kNRaw, area = gs & 1u;
+    const uint32_t cnt = (K - s * CH) < (uint32_t)CH ? (K - s * CH) : CH;
+    const bool ok = mbar_wait(S.bars + slot, (gs / kNRaw) & 1u, kWaitNs);
+    if (!P.tma) {
+      copy_stage_plain<CH, TY>(P, G, S, s, slot, cnt);
+      __syncthreads();
+    }
+    uint32_t *tb = table + area * (CH * kTileD);
+#pragma unroll
+    for (int r = 0; r < Delays::R; ++r) {
+      const uint32_t idx = tid + r * kThreads;
+      if (idx < cnt * kTileD) {
+        const uint32_t ch = idx / kTileD;
+        const uint32_t o = delays.offset(P, G, S, r, s, slot, t0, d0);
+        tb[idx] = (slot * CH + ch) * L.raw_stride + 4u * o;
+      }
+    }
+    if (s + 1 < nst)
+      delays.load(P, G, s + 1, dtile, (K - (s + 1) * CH) < (uint32_t)CH ? (K - (s + 1) * CH) : CH);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) atomicOr(P.status, kStatusTimeout);
+      const uint32_t last = (s + kAhead) < nst ? (s + kAhead) : nst;
+      drain_stages(S, sc, s, last);
+      return false;
+    }
+    if (ty == 0 && s + kAhead < nst)
+      issue_stage<CH>(P, G, S, s + kAhead, gs + kAhead, t0, d0, dtile, tx);
+
+    const uint32_t *tbt = tb + ty * NDT;
+    for (uint32_t ch = 0; ch < cnt; ++ch) {
+      uint32_t b[NDT];
+#pragma unroll
+      for (int j = 0; j < NDT; ++j) b[j] = raws + tbt[ch * kTileD + j];
+#pragma unroll
+      for (int j = 0; j < NDT; ++j)
+#pragma unroll
+        for (int i = 0; i < NS; ++i) acc[j][i] += lds_u32(b[j] + 128u * i);
+      if (++since == P.flush_rows) {
+        widen();
+        since = 0;
+      }
+    }
+  }
+  sc += nst;
+  widen();
+
+  const bool hi_ok = (g % P.pair_groups) * 2u + 1u < P.pair_d1;
+#pragma unroll
+  for (int j = 0; j < NDT; ++j) {
+    const uint32_t d = d0 + ty * NDT + j;
+    if (d >= P.nr_dms) continue;
+    float *orow = P.out + G.out_offset + (uint64_t)d * P.out_dm_stride;
+#pragma unroll
+    for (int i = 0; i < NS; ++i) {
+      const uint32_t t = t0 + tx + 32u * i;
+      if (t < P.nr_samples) {
+        orow[t] = (float)tlo[j][i];
+        if (hi_ok) orow[P.pair_stride + t] = (float)thi[j][i];
+      }
     }
   }
   return true;

@@ -105,6 +105,19 @@ struct ProblemDesc {
   // {sum, sum of squares, peak << 32 | (0xffffffff - sample)}, accumulated
   // with atomics by the shared-partial-sum kernel.
   unsigned long long *accum;
+  // Packed subband intermediate (0: float rows).  Step one with packed = 1
+  // writes, per pair of coarse DMs (2p, 2p + 1), one 32-bit word per sample:
+  // the exact sum of DM 2p in the low 16 bits, of DM 2p + 1 in the high 16
+  // (0 where 2p + 1 is past the last coarse DM); row (beam, p, subband) at
+  // ((beam * pairs + p) * subbands + subband) * out_row words.  The pair
+  // kernel (step two) reads those rows: group (synthesized beam, p) writes
+  // DM rows d of coarse DM 2p at out_offset + d * out_dm_stride and of coarse
+  // DM 2p + 1 pair_stride floats further on.
+  uint32_t packed;
+  uint32_t pair_groups;   // pairs of coarse DMs (groups per synthesized beam)
+  uint32_t pair_d1;       // coarse DMs
+  uint32_t flush_rows;    // rows summed in 16-bit lanes before widening
+  uint64_t pair_stride;   // floats from a coarse DM 2p row to its 2p + 1 row
 };
 
 // One entry of the kernel registry: a compiled tile configuration.
@@ -125,7 +138,7 @@ struct KernelInfo {
                  cudaStream_t stream);
 };
 
-enum { kFamilySwar8 = 0, kFamilyScalar = 1, kFamilyShared8 = 2 };
+enum { kFamilySwar8 = 0, kFamilyScalar = 1, kFamilyShared8 = 2, kFamilyPair16 = 3 };
 
 // Registry of compiled configurations (dd_kernels.cu).
 const KernelInfo *kernel_registry(int *count);

@@ -33,6 +33,17 @@ __global__ void __launch_bounds__(32 * TY, (TY >= 8 ? 2 : 4))
   (void)scalar_tile<T, NS, NDT, TY, CH>(P, P.groups[g], dtile, ttile, smem, L, sc);
 }
 
+template <int NS, int NDT, int TY, int CH>
+__global__ void __launch_bounds__(32 * TY, (TY >= 8 ? 2 : 4))
+    pair_kernel(const ProblemDesc P) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  const SmemLayout L = make_layout(kFamilyPair16, P.win_samples, 32, CH, TY * NDT);
+  init_barriers(smem, L, CH);
+  uint32_t g, dtile, ttile, sc = 0;
+  decode_tile(P, blockIdx.x, g, dtile, ttile);
+  (void)pair_tile<NS, NDT, TY, CH>(P, g, P.groups[g], dtile, ttile, smem, L, sc);
+}
+
 template <int NW, int ND, int TY>
 __global__ void __launch_bounds__(32 * TY, (TY >= 16 ? 1 : 2))
     shared8_kernel(const ProblemDesc P) {
@@ -66,6 +77,11 @@ void launch_scalar(const ProblemDesc &P, unsigned grid, size_t smem,
   scalar_kernel<T, NS, NDT, TY, CH><<<grid, 32 * TY, smem, stream>>>(P);
 }
 
+template <int NS, int NDT, int TY, int CH>
+void launch_pair(const ProblemDesc &P, unsigned grid, size_t smem, cudaStream_t stream) {
+  pair_kernel<NS, NDT, TY, CH><<<grid, 32 * TY, smem, stream>>>(P);
+}
+
 template <int NW, int ND, int TY>
 void launch_shared8(const ProblemDesc &P, unsigned grid, size_t smem,
                     cudaStream_t stream) {
@@ -92,6 +108,17 @@ void launch_shared8(const ProblemDesc &P, unsigned grid, size_t smem,
    kSharedRows, 32 * TY, 64 * NW, TY * ND, 0,                                 \
    reinterpret_cast<const void *>(&shared8_kernel<NW, ND, TY>),              \
    &launch_shared8<NW, ND, TY>}
+
+// Pair tiles (packed subband step two): items_t = samples per thread, items_d
+// = DMs per thread.  Not in the registry: they read only the packed
+// intermediate that a subband pipeline's own step one writes.
+#define DD_PAIR(NS, NDT, TY, CH)                                              \
+  {"pair16_i" #NS "_d" #NDT "_w" #TY "_c" #CH, kFamilyPair16, 32, NS, NDT,   \
+   TY, CH, 32 * TY, 32 * NS, TY * NDT, 0,                                     \
+   reinterpret_cast<const void *>(&pair_kernel<NS, NDT, TY, CH>),            \
+   &launch_pair<NS, NDT, TY, CH>}
+
+const KernelInfo *pair_kernels(int *count);
 
 // Parts of the registry, one per translation unit (compiled in parallel).
 const KernelInfo *kernels_swar8_a(int *count);

@@ -8,7 +8,8 @@
 //   1. copy the S new samples from the stream's pinned staging buffer into
 //      the ring after the tail,
 //   2. dedisperse the ring (one single-step plan, or step one into a device
-//      intermediate and step two from it),
+//      intermediate and step two from it; the intermediate is packed, two
+//      coarse DMs' 16-bit sums per word, where the sums fit 16 bits),
 //   3. copy the output's valid samples into the pinned output buffer,
 //   4. carry the last `tail` samples of every row to the front of the ring.
 //
@@ -31,6 +32,9 @@
 
 namespace dd {
 void set_last_error(const char *message);
+bool subband_packable(const dd_observation *o, const uint32_t *zapped, uint32_t bits);
+bool subband_try_pack(dd_plan *one, dd_plan *two, const dd_observation *o, const uint32_t *zapped,
+                      uint32_t bits, int pair_kernel);
 }
 
 namespace {
@@ -72,6 +76,7 @@ struct Geometry {
   dd_observation two;   // step two (subband mode)
   uint32_t tail = 0;    // carried samples
   dd_layout ring{}, mid{}, out{};
+  bool packed = false;  // subband mode: packed step-one intermediate
 };
 
 dd_status geometry(const dd_observation *o, int subband, uint32_t bits, uint32_t padding,
@@ -126,6 +131,7 @@ dd_status geometry(const dd_observation *o, int subband, uint32_t bits, uint32_t
     if (!st) st = dd_get_layout(&g->two, DD_STEP_TWO, 32, padding, nullptr, &g->out);
     if (st) return st;
     g->mid = g->ring;
+    g->packed = dd::subband_packable(&g->one, zapped, bits);
   }
   if (g->tail > S) return fail(DD_ERR_UNSUPPORTED, "max delay %u exceeds the batch of %u samples", g->tail, S);
   if (o->nr_beams != 1 || o->nr_synthesized_beams != 1)
@@ -168,9 +174,17 @@ void release(dd_stream *s) {
   if (s->h_out) cudaFreeHost(s->h_out);
 }
 
+// Bytes of the step-one intermediate: the float rows, or half as many packed
+// rows (pairs of coarse DMs) when the sums fit 16 bits.
+uint64_t mid_bytes(const Geometry &g) {
+  const uint64_t D1 = g.one.nr_dms_subbanding;
+  if (!g.packed || D1 == 0) return g.ring.output_bytes;
+  return g.ring.output_bytes / D1 * ((D1 + 1) / 2);
+}
+
 uint64_t total_bytes(const Geometry &g, int subband) {
   uint64_t b = g.ring.input_bytes + g.out.output_bytes;
-  if (subband) b += g.ring.output_bytes;  // step-one intermediate
+  if (subband) b += mid_bytes(g);  // step-one intermediate
   return b;
 }
 
@@ -253,6 +267,8 @@ dd_status dd_stream_create(dd_stream **out, const dd_observation *obs, int subba
     std::vector<uint32_t> map(g.out.mapping_row_elems, 0);
     if (!st) st = dd_plan_set_shifts(s->plan2, shifts_step_two, g.two.nr_subbands);
     if (!st) st = dd_plan_set_beam_mapping(s->plan2, map.data(), map.size());
+    // The packed intermediate where the step-one sums fit 16 bits.
+    if (!st) s->g.packed = dd::subband_try_pack(s->plan1, s->plan2, &g.one, zapped, input_bits, 0);
   }
   // Build the plans' tables now (they are built on first use), so that the
   // push recorded as a graph below launches only kernels.
@@ -266,7 +282,7 @@ dd_status dd_stream_create(dd_stream **out, const dd_observation *obs, int subba
   cudaError_t e = cudaMalloc(&s->d_ring, g.ring.input_bytes);
   if (e == cudaSuccess) e = cudaMemset(s->d_ring, 0, g.ring.input_bytes);
   if (e == cudaSuccess) e = cudaMalloc(&s->d_out, g.out.output_bytes);
-  if (e == cudaSuccess && s->subband) e = cudaMalloc(&s->d_mid, g.ring.output_bytes);
+  if (e == cudaSuccess && s->subband) e = cudaMalloc(&s->d_mid, mid_bytes(g));
   if (e == cudaSuccess) e = cudaHostAlloc(&s->h_in, s->in_row_bytes * C, cudaHostAllocDefault);
   if (e == cudaSuccess) e = cudaMemset(s->d_out, 0, g.out.output_bytes);
   if (e == cudaSuccess)

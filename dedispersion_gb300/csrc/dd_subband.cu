@@ -1,0 +1,298 @@
+// dd_subband.cu -- the subband method as one pipeline on the device: step one
+// then step two, the intermediate kept in device memory the pipeline owns.
+//
+// The reference computes the two steps as separate calls with a float
+// intermediate of [beam][coarse DM][subband][S1] (include/Dedispersion.hpp:
+// 111-176); its drivers never chain them (src/DedispersionTest.cpp runs one
+// step per invocation).  Here, when the step-one sums fit 16 bits (live
+// channels per subband x (2^bits - 1) <= 65535, e.g. up to 257 channels of
+// 8-bit input), the intermediate is packed: one 32-bit word per sample holds
+// the exact sums of two coarse DMs (ProblemDesc::packed).  That halves its
+// bytes (101 MB instead of 202 MB at 1536 channels, 32 subbands, 64 coarse
+// DMs, 24649 samples, small enough to stay largely in the 129 MB L2 between
+// the steps), and step two's pair tile adds both coarse DMs with one load and
+// one add.
+// Sums are integers below 2^24 either way, so the output equals the
+// reference's float step one followed by its float step two bit for bit.
+// Otherwise (16-bit or float input, or wider subbands) the pipeline runs the
+// two float steps.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <vector>
+
+#include "../../include/dedisp_gb300.h"
+#include "dd_kernels.cuh"
+
+namespace dd {
+void set_last_error(const char *message);
+void plan_set_packed(dd_plan *p, const KernelInfo *k, uint32_t flush_rows);
+void plan_clear_packed(dd_plan *p);
+bool plan_ready(const dd_plan *p);
+
+// Largest step-one sum: live channels of the fullest subband x the largest
+// sample of `bits`-bit input (0 when the width has no integer bound).
+uint64_t subband_largest_sum(const dd_observation *o, const uint32_t *zapped, uint32_t bits) {
+  const uint32_t C = o->nr_channels, SB = o->nr_subbands;
+  if (SB == 0 || bits > 16) return 0;
+  const uint32_t cps = C / SB;
+  uint32_t live_max = 0;
+  for (uint32_t sb = 0; sb < SB; sb++) {
+    uint32_t live = 0;
+    for (uint32_t c = sb * cps; c < (sb + 1) * cps; c++) live += (zapped && zapped[c]) ? 0u : 1u;
+    live_max = std::max(live_max, live);
+  }
+  return (uint64_t)live_max * ((1ull << bits) - 1);
+}
+
+// Whether the packed intermediate holds this shape's step-one sums exactly.
+bool subband_packable(const dd_observation *o, const uint32_t *zapped, uint32_t bits) {
+  return bits <= 8 && o->nr_subbands && subband_largest_sum(o, zapped, bits) <= 0xFFFFu;
+}
+
+// Turns step plans `one` and `two` (tables set) into a packed pair where the
+// sums fit and both build (else leaves them as float steps).  Returns whether
+// they are packed.
+bool subband_try_pack(dd_plan *one, dd_plan *two, const dd_observation *o, const uint32_t *zapped,
+                      uint32_t bits, int pair_kernel) {
+  if (!subband_packable(o, zapped, bits)) return false;
+  const uint64_t big = subband_largest_sum(o, zapped, bits);
+  const uint32_t flush = (uint32_t)std::max<uint64_t>(1, big ? 0xFFFFu / big : 0xFFFFu);
+  int n = 0;
+  const KernelInfo *pk = pair_kernels(&n);
+  plan_set_packed(one, nullptr, 0);
+  plan_set_packed(two, &pk[std::min(std::max(pair_kernel, 0), n - 1)], flush);
+  if (plan_ready(one) && plan_ready(two)) return true;
+  plan_clear_packed(one);
+  plan_clear_packed(two);
+  return false;
+}
+}  // namespace dd
+
+namespace {
+
+dd_status fail(dd_status code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  dd::set_last_error(buf);
+  return code;
+}
+
+dd_status cuda_fail(cudaError_t e, const char *what) {
+  (void)cudaGetLastError();
+  if (e == cudaErrorMemoryAllocation)
+    return fail(DD_ERR_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
+  return fail(DD_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define DDS_CUDA(call, what)                           \
+  do {                                                 \
+    cudaError_t e_ = (call);                           \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+}  // namespace
+
+struct dd_subband {
+  int device = 0;
+  dd_observation obs{};
+  uint32_t bits = 8, padding = 0;
+  dd_plan *one = nullptr, *two = nullptr;
+  bool packed = false;
+  bool ready = false;
+  int pair_kernel = 0;  // index into dd::pair_kernels
+  void *inter = nullptr;  // step-one output (packed or float)
+  size_t inter_bytes = 0;
+  std::vector<float> shifts, shifts2;
+  std::vector<uint32_t> zapped, mapping;
+};
+
+namespace {
+
+void drop_plans(dd_subband *s) {
+  if (s->one) dd_plan_destroy(s->one);
+  if (s->two) dd_plan_destroy(s->two);
+  s->one = s->two = nullptr;
+}
+
+dd_status make_plans(dd_subband *s) {
+  drop_plans(s);
+  dd_status st = dd_plan_create(&s->one, &s->obs, DD_STEP_ONE, s->bits, s->padding, nullptr,
+                                s->device);
+  if (!st) st = dd_plan_create(&s->two, &s->obs, DD_STEP_TWO, 32, s->padding, nullptr, s->device);
+  if (!st) st = dd_plan_set_shifts(s->one, s->shifts.data(), s->shifts.size());
+  if (!st) st = dd_plan_set_zapped(s->one, s->zapped.data(), s->zapped.size());
+  if (!st) st = dd_plan_set_shifts(s->two, s->shifts2.data(), s->shifts2.size());
+  if (!st) st = dd_plan_set_beam_mapping(s->two, s->mapping.data(), s->mapping.size());
+  return st;
+}
+
+// Builds both plans, packed where the sums fit, and sizes the intermediate.
+dd_status build(dd_subband *s) {
+  s->ready = false;
+  dd_status st = make_plans(s);
+  if (st) return st;
+  s->packed = dd::subband_try_pack(s->one, s->two, &s->obs, s->zapped.data(), s->bits,
+                                   s->pair_kernel);
+  uint64_t adds = 0;  // builds the tables, reporting why they are invalid
+  st = dd_plan_adds(s->one, &adds);
+  if (!st) st = dd_plan_adds(s->two, &adds);
+  if (st) return st;
+  dd_layout lay;
+  st = dd_get_layout(&s->obs, DD_STEP_ONE, s->bits, s->padding, nullptr, &lay);
+  if (st) return st;
+  const uint64_t D1 = s->obs.nr_dms_subbanding;
+  size_t bytes = lay.output_bytes;
+  if (s->packed && D1) bytes = lay.output_bytes / D1 * ((D1 + 1) / 2);
+  if (bytes > s->inter_bytes) {
+    if (s->inter) cudaFree(s->inter);
+    s->inter = nullptr;
+    s->inter_bytes = 0;
+    DDS_CUDA(cudaSetDevice(s->device), "select device");
+    DDS_CUDA(cudaMalloc(&s->inter, std::max<size_t>(bytes, 16)), "allocate intermediate");
+    s->inter_bytes = bytes;
+  }
+  s->ready = true;
+  return DD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+dd_status dd_subband_create(dd_subband **pipeline, const dd_observation *obs,
+                            uint32_t input_bits, uint32_t padding, int device) {
+  if (!pipeline || !obs) return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
+  *pipeline = nullptr;
+  if (obs->nr_subbands == 0) return fail(DD_ERR_INVALID_ARGUMENT, "observation has no subbands");
+  // Validate geometry, bits and device through the step plans themselves.
+  dd_plan *probe = nullptr;
+  dd_status st = dd_plan_create(&probe, obs, DD_STEP_ONE, input_bits, padding, nullptr, device);
+  if (st) return st;
+  dd_plan_destroy(probe);
+  st = dd_plan_create(&probe, obs, DD_STEP_TWO, 32, padding, nullptr, device);
+  if (st) return st;
+  dd_plan_destroy(probe);
+  dd_subband *s = new dd_subband();
+  s->device = device;
+  s->obs = *obs;
+  s->bits = input_bits;
+  s->padding = padding;
+  *pipeline = s;
+  return DD_OK;
+}
+
+dd_status dd_subband_set_tables(dd_subband *s, const float *shifts, size_t n_shifts,
+                                const float *shifts_step_two, size_t n_shifts2,
+                                const uint32_t *zapped, size_t n_zapped,
+                                const uint32_t *beam_mapping, size_t n_mapping) {
+  if (!s || !shifts || !shifts_step_two || !zapped || !beam_mapping)
+    return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (n_shifts < s->obs.nr_channels || n_zapped < s->obs.nr_channels ||
+      n_shifts2 < s->obs.nr_subbands)
+    return fail(DD_ERR_INVALID_ARGUMENT, "tables shorter than %u channels / %u subbands",
+                s->obs.nr_channels, s->obs.nr_subbands);
+  s->shifts.assign(shifts, shifts + n_shifts);
+  s->shifts2.assign(shifts_step_two, shifts_step_two + n_shifts2);
+  s->zapped.assign(zapped, zapped + n_zapped);
+  s->mapping.assign(beam_mapping, beam_mapping + n_mapping);
+  return build(s);
+}
+
+dd_status dd_subband_run(dd_subband *s, const void *d_input, float *d_output, void *stream) {
+  if (!s) return fail(DD_ERR_INVALID_ARGUMENT, "pipeline is NULL");
+  if (!s->ready) return fail(DD_ERR_INVALID_ARGUMENT, "pipeline has no tables");
+  dd_status st = dd_plan_run(s->one, d_input, static_cast<float *>(s->inter), stream);
+  if (!st) st = dd_plan_run(s->two, s->inter, d_output, stream);
+  return st;
+}
+
+dd_status dd_subband_check(dd_subband *s, void *stream) {
+  if (!s) return fail(DD_ERR_INVALID_ARGUMENT, "pipeline is NULL");
+  if (!s->ready) return fail(DD_ERR_INVALID_ARGUMENT, "pipeline has no tables");
+  dd_status st = dd_plan_check(s->one, stream);
+  if (!st) st = dd_plan_check(s->two, stream);
+  return st;
+}
+
+dd_status dd_subband_info(const dd_subband *s, int *packed, uint64_t *intermediate_bytes) {
+  if (!s) return fail(DD_ERR_INVALID_ARGUMENT, "pipeline is NULL");
+  if (!s->ready) return fail(DD_ERR_INVALID_ARGUMENT, "pipeline has no tables");
+  if (packed) *packed = s->packed ? 1 : 0;
+  if (intermediate_bytes) *intermediate_bytes = s->inter_bytes;
+  return DD_OK;
+}
+
+dd_status dd_subband_set_pair_kernel(dd_subband *s, int index) {
+  if (!s) return fail(DD_ERR_INVALID_ARGUMENT, "pipeline is NULL");
+  int n = 0;
+  (void)dd::pair_kernels(&n);
+  if (index < 0 || index >= n)
+    return fail(DD_ERR_INVALID_ARGUMENT, "pair kernel %d out of range (0..%d)", index, n - 1);
+  s->pair_kernel = index;
+  return s->shifts.empty() ? DD_OK : build(s);
+}
+
+int dd_subband_pair_kernel_count(void) {
+  int n = 0;
+  (void)dd::pair_kernels(&n);
+  return n;
+}
+
+dd_status dd_subband_destroy(dd_subband *s) {
+  if (!s) return DD_OK;
+  drop_plans(s);
+  if (s->inter) {
+    cudaSetDevice(s->device);
+    cudaFree(s->inter);
+  }
+  delete s;
+  return DD_OK;
+}
+
+dd_status dd_subband_dedispersion(const dd_observation *obs, const uint32_t *zapped,
+                                  const uint32_t *beam_mapping, const void *input, float *output,
+                                  const float *shifts, const float *shifts_step_two,
+                                  uint32_t padding, uint32_t input_bits) {
+  if (!obs || !zapped || !beam_mapping || !input || !output || !shifts || !shifts_step_two)
+    return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
+  dd_layout l1, l2;
+  dd_status st = dd_get_layout(obs, DD_STEP_ONE, input_bits, padding, nullptr, &l1);
+  if (!st) st = dd_get_layout(obs, DD_STEP_TWO, 32, padding, nullptr, &l2);
+  if (st) return st;
+  dd_subband *s = nullptr;
+  st = dd_subband_create(&s, obs, input_bits, padding, 0);
+  if (st) return st;
+  void *d_in = nullptr, *d_out = nullptr;
+  cudaStream_t stream = nullptr;
+  auto done = [&](dd_status code) {
+    if (d_in) cudaFree(d_in);
+    if (d_out) cudaFree(d_out);
+    if (stream) cudaStreamDestroy(stream);
+    dd_subband_destroy(s);
+    return code;
+  };
+  st = dd_subband_set_tables(s, shifts, l1.shifts_elems, shifts_step_two, l2.shifts_elems, zapped,
+                             l1.zapped_elems, beam_mapping,
+                             (size_t)obs->nr_synthesized_beams * l2.mapping_row_elems);
+  if (st) return done(st);
+  cudaError_t e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&d_in, std::max<uint64_t>(l1.input_bytes, 16));
+  if (e == cudaSuccess) e = cudaMalloc(&d_out, std::max<uint64_t>(l2.output_bytes, 16));
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_in, input, l1.input_bytes, cudaMemcpyHostToDevice, stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_out, 0, l2.output_bytes, stream);
+  if (e != cudaSuccess) return done(cuda_fail(e, "stage subband buffers"));
+  st = dd_subband_run(s, d_in, static_cast<float *>(d_out), stream);
+  if (st) return done(st);
+  e = cudaMemcpyAsync(output, d_out, l2.output_bytes, cudaMemcpyDeviceToHost, stream);
+  if (e != cudaSuccess) return done(cuda_fail(e, "copy output"));
+  return done(dd_subband_check(s, stream));
+}
+
+}  // extern "C"

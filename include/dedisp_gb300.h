@@ -211,6 +211,47 @@ dd_status dd_subband_dedispersion_step_two(const dd_observation *obs,
                                            const float *shifts,
                                            uint32_t padding);
 
+/* ---- subband pipeline: step one then step two on the device ------------- */
+/* No counterpart in the reference, which runs the two steps as separate calls
+ * (the two declarations above) with a float intermediate.  A pipeline owns
+ * the intermediate.  When every subband's step-one sums fit 16 bits (live
+ * channels per subband x (2^bits - 1) <= 65535) it is packed, one 32-bit
+ * word per sample holding two coarse DMs' exact sums: half the bytes, and
+ * step two adds both with one load.  Otherwise it runs the two float steps.
+ * The output equals step one followed by step two bit for bit, in step two's
+ * layout [synthesized beam][DM1 * DM2][pad(S)]; input in step one's. */
+typedef struct dd_subband dd_subband;
+dd_status dd_subband_create(dd_subband **pipeline, const dd_observation *obs,
+                            uint32_t input_bits, uint32_t padding, int device);
+/* Shift tables of both steps (getShifts, getShiftsStepTwo), the zapped mask
+ * (step one) and the beam mapping (step two); builds both steps' tables. */
+dd_status dd_subband_set_tables(dd_subband *pipeline, const float *shifts,
+                                size_t n_shifts, const float *shifts_step_two,
+                                size_t n_shifts_step_two,
+                                const uint32_t *zapped, size_t n_zapped,
+                                const uint32_t *beam_mapping, size_t n_mapping);
+/* Enqueue both steps on `stream` (device pointers). */
+dd_status dd_subband_run(dd_subband *pipeline, const void *d_input,
+                         float *d_output, void *stream);
+/* Synchronize `stream` and report a device-side timeout of either step. */
+dd_status dd_subband_check(dd_subband *pipeline, void *stream);
+/* Whether the intermediate is packed, and its device bytes. */
+dd_status dd_subband_info(const dd_subband *pipeline, int *packed,
+                          uint64_t *intermediate_bytes);
+/* Tile configuration of the packed step two (0 .. count - 1; 0 default). */
+dd_status dd_subband_set_pair_kernel(dd_subband *pipeline, int index);
+int dd_subband_pair_kernel_count(void);
+dd_status dd_subband_destroy(dd_subband *pipeline);
+/* Both steps on host buffers, synchronously (input as for step one, output
+ * as for step two; the intermediate never leaves the device). */
+dd_status dd_subband_dedispersion(const dd_observation *obs,
+                                  const uint32_t *zapped,
+                                  const uint32_t *beam_mapping,
+                                  const void *input, float *output,
+                                  const float *shifts,
+                                  const float *shifts_step_two,
+                                  uint32_t padding, uint32_t input_bits);
+
 /* Single-step dedispersion that allocates no device memory.  It has no
  * counterpart in the reference.  It is for callers that cannot call
  * cudaMalloc where they dedisperse: a real-time loop that must not block
