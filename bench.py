@@ -269,6 +269,81 @@ def bench_ingest(torch, inp, lay, obs, stream):
                     "descending-frequency file order reversed on the way"}
 
 
+def bench_subband(torch, device: int, steps: int, hbm_peak: float, peak_adds: float):
+    """Config 2 in subband mode (1536 ch in 32 subbands, 64 coarse DMs at 6.4
+    x 32 fine DMs at 0.2, 24576 samples, uint8 N(128, 20), 5 % zapped): the
+    subband pipeline (packed 16-bit intermediate, dd_subband_run) against the
+    engine's two float steps back to back, outputs compared bit for bit."""
+    import dedispersion_gb300 as dd
+    from dedispersion_gb300 import synthetic as syn
+    obs = syn.large_observation(PADDING, subbands=True)
+    sh1, sh2 = dd.getShifts(obs, PADDING), dd.getShiftsStepTwo(obs, PADDING)
+    zapped = syn.zapped_mask(1536, 0.05, 7, PADDING)
+    mapping = syn.identity_mapping(obs, PADDING, subbands=True)
+    inp = syn.make_input(obs, 8, PADDING, seed=3, mode=dd.DD_STEP_ONE, mean=128.0, sigma=20.0)
+    l1 = dd.layout(obs, dd.DD_STEP_ONE, 8, PADDING)
+    l2 = dd.layout(obs, dd.DD_STEP_TWO, 32, PADDING)
+    dev = f"cuda:{device}"
+    nbuf = 4  # 4 x 45 MB inputs: each step reads its input from HBM
+    d_in = [torch.from_numpy(inp).to(dev) for _ in range(nbuf)]
+    out = torch.empty(l2.output_bytes // 4, dtype=torch.float32, device=dev)
+    ref = torch.empty_like(out)
+    pipe = dd.SubbandPipeline(obs, 8, PADDING, device=device)
+    pipe.setTables(sh1, sh2, zapped, mapping)
+    one = dd.Plan(obs, dd.DD_STEP_ONE, 8, PADDING, device=device)
+    one.setShifts(sh1)
+    one.setZappedChannels(zapped)
+    two = dd.Plan(obs, dd.DD_STEP_TWO, 32, PADDING, device=device)
+    two.setShifts(sh2)
+    two.setBeamMapping(mapping)
+    inter = torch.empty(l1.output_bytes // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def timed(fn):
+        for i in range(3):
+            fn(i)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(steps):
+            fn(i)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / steps
+
+    t_pipe = timed(lambda i: pipe.run(d_in[i % nbuf], out, stream))
+    pipe.check(stream)
+    t_float = timed(lambda i: (one.run(d_in[i % nbuf], inter, stream),
+                               two.run(inter, ref, stream)))
+    two.check(stream)
+    pipe.run(d_in[0], out, stream)
+    one.run(d_in[0], inter, stream)
+    two.run(inter, ref, stream)
+    torch.cuda.synchronize()
+    exact = bool(torch.equal(out, ref))
+    info = pipe.info()
+    D1, D2, SB = obs.getNrDMs(True), obs.getNrDMs(), obs.getNrSubbands()
+    S, S1 = obs.getNrSamplesPerBatch(), obs.getNrSamplesPerBatch(True)
+    live = int((zapped[:1536] == 0).sum())
+    units = D1 * D2 * S
+    adds = live * D1 * S1 + SB * D1 * D2 * S  # step one + step two, algorithmic
+    hbm_bytes = inp.nbytes + 2 * info["intermediate_bytes"] + D1 * D2 * S * 4
+    for x in (pipe, one, two):
+        x.close()
+    return {"value": units / t_pipe, "unit": UNIT, "ms_per_batch": t_pipe * 1e3,
+            "float_steps_value": units / t_float, "float_steps_ms": t_float * 1e3,
+            "speedup_vs_float_steps": t_float / t_pipe, "bit_exact_vs_float_steps": exact,
+            "packed": info["packed"], "intermediate_bytes": info["intermediate_bytes"],
+            "adds_per_batch": adds, "adds_frac": adds / t_pipe / peak_adds,
+            "hbm_bytes_upper": hbm_bytes,
+            "hbm_frac_upper": hbm_bytes / t_pipe / 1e9 / hbm_peak,
+            "gpu_launches_per_batch": 2,
+            "workload": "1536 ch in 32 subbands (5% zapped), 64 coarse DMs at 6.4 x 32 fine "
+                        "DMs at 0.2 = 2048 DMs, 24576 samples, uint8 N(128, 20)",
+            "note": "hbm_bytes_upper counts the intermediate written and read once through "
+                    "HBM; the part that stays in L2 makes the true traffic lower"}
+
+
 def bench_batched(torch, device: int, reps: int = 3, count: int = 40):
     """40 uneven beams (384/1536 ch, 8192-32768 samples, 512-4096 DMs, steps
     0.1-0.5, 2/4/8-bit uniform input) in one CUDA graph launch (the beams'
@@ -501,8 +576,16 @@ def main():
     t_e2e = max_over_ranks(time.perf_counter() - t, pg, f"cuda:{local}")
     e2e_value = job_value(world, e2e_steps, D, S, t_e2e)
 
+    sm_mhz = clocks.get("sm_mhz") or 2070.0
+    peak_adds = SMS * LANES * sm_mhz * 1e6
+    hbm_peak = 6784.2
+    try:
+        hbm_peak = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"]
+    except Exception:
+        pass
     detect = bench_detect(torch, plan, d_in, d_out, stream, D, S, args.steps)
     ingest_line = bench_ingest(torch, inp, lay, obs, stream)
+    subband = bench_subband(torch, local, max(10, min(args.steps, 50)), hbm_peak, peak_adds)
     batched = bench_batched(torch, local) if not args.no_batched else None
     served = bench_served(local) if not args.no_served else None
 
@@ -511,14 +594,7 @@ def main():
     # roofline of the plain kernel
     adds_per_launch = D * S * live
     achieved_adds = adds_per_launch / per_launch_s
-    sm_mhz = clocks.get("sm_mhz") or 2070.0
-    peak_adds = SMS * LANES * sm_mhz * 1e6
     compulsory = inp.nbytes // 1 + D * S * 4
-    hbm_peak = 6784.2
-    try:
-        hbm_peak = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"]
-    except Exception:
-        pass
     traffic = read_profile_traffic()
     executed_adds = plan.adds()
     kernel_name = next((k.name for k in dd.kernels()
@@ -564,6 +640,7 @@ def main():
         "gpu_launches": args.steps * plan.launches(),
         "detect": detect,
         "ingest": ingest_line,
+        "subband": subband,
         "batched": batched,
         "served": served,
     }
