@@ -260,6 +260,30 @@ void subbandDedispersionStepTwo(AstroData::Observation &observation,
                                          output.data(), shifts.data(), padding));
 }
 
+// subbandDedispersionStepOne followed by subbandDedispersionStepTwo in one
+// call (no reference counterpart): the intermediate stays on the device,
+// packed as exact 16-bit sums of coarse-DM pairs where they fit; `output`
+// equals the two calls' output bit for bit.  Input as for step one, output as
+// for step two.
+template <typename I, typename L, typename O>
+void subbandDedispersion(AstroData::Observation &observation,
+                         const std::vector<unsigned int> &zappedChannels,
+                         const std::vector<unsigned int> &beamMapping, const std::vector<I> &input,
+                         std::vector<O> &output, const std::vector<float> &shifts,
+                         const std::vector<float> &shiftsStepTwo, const unsigned int padding,
+                         const uint8_t inputBits) {
+  detail::check_types<I, L, O>();
+  const unsigned int bits = inputBits < 8 ? inputBits : detail::storage_bits<I>();
+  dd_layout one, two;
+  check(dd_get_layout(&observation.c(), DD_STEP_ONE, bits, padding, nullptr, &one));
+  check(dd_get_layout(&observation.c(), DD_STEP_TWO, 32, padding, nullptr, &two));
+  detail::check_size(input.size() * sizeof(I), one.input_bytes, "input");
+  detail::check_size(output.size() * sizeof(O), two.output_bytes, "output");
+  check(dd_subband_dedispersion(&observation.c(), zappedChannels.data(), beamMapping.data(),
+                                input.data(), output.data(), shifts.data(),
+                                shiftsStepTwo.data(), padding, bits));
+}
+
 // Loads every "device nrDMs split local unroll tD0 tD1 tD2 iD0 iD1 iD2"
 // line; lines not starting with a letter are skipped and the first line of a
 // (device, nrDMs) pair wins.  Throws AstroData::FileError if the file cannot

@@ -11,9 +11,9 @@ CUDA = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 SRC = ROOT / "tests" / "cpp" / "dedispersion_test.cpp"
 
 
-def compile_test(out: Path, syntax_only: bool = False) -> None:
+def compile_test(out: Path, syntax_only: bool = False, src: Path = SRC) -> None:
     cmd = ["g++", "-std=c++14", "-O2", "-Wall", "-Wno-unused-result", f"-I{ROOT / 'include'}",
-           f"-I{CUDA / 'include'}", str(SRC)]
+           f"-I{CUDA / 'include'}", str(src)]
     if syntax_only:
         cmd += ["-fsyntax-only"]
     else:
@@ -26,6 +26,7 @@ def compile_test(out: Path, syntax_only: bool = False) -> None:
 
 def test_header_compiles_as_cpp14(engine):
     compile_test(Path("/dev/null"), syntax_only=True)
+    compile_test(Path("/dev/null"), syntax_only=True, src=ROOT / "tests" / "cpp" / "subband_test.cpp")
 
 
 def test_header_declares_the_reference_surface():
@@ -33,7 +34,7 @@ def test_header_declares_the_reference_surface():
     for name in ["class Observation", "class DedispersionConf", "getShifts(", "getShiftsStepTwo(",
                  "void dedispersion(", "void subbandDedispersionStepOne(",
                  "void subbandDedispersionStepTwo(", "readTunedDedispersionConf(",
-                 "tunedDedispersionConf"]:
+                 "tunedDedispersionConf", "void subbandDedispersion("]:
         assert name in text, name
 
 
@@ -69,5 +70,18 @@ def test_dedispersion_test_twin_passes(gpu, oracle, tmp_path, run):
     if "-step_two" not in run:
         args += ["-zapped_channels", str(zfile)]
     proc = subprocess.run(args, capture_output=True, text=True, timeout=300)
+    assert proc.returncode == 0, proc.stdout + proc.stderr
+    assert "TEST PASSED." in proc.stdout
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("argv", [["256", "8", "16", "16", "8", "1", "1", "3"],
+                                  ["512", "4", "7", "12", "8", "2", "3", "5"],
+                                  ["256", "8", "9", "16", "4", "2", "2", "7"]],
+                         ids=["8bit", "odd_coarse_multibeam", "4bit"])
+def test_subband_one_call_matches_oracle(gpu, oracle, tmp_path, argv):
+    exe = tmp_path / "subband_test"
+    compile_test(exe, src=ROOT / "tests" / "cpp" / "subband_test.cpp")
+    proc = subprocess.run([str(exe), *argv], capture_output=True, text=True, timeout=300)
     assert proc.returncode == 0, proc.stdout + proc.stderr
     assert "TEST PASSED." in proc.stdout
