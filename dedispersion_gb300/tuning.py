@@ -128,7 +128,8 @@ def sweep(obs, mode: int, bits: int, padding: int, shifts, zapped=None, mapping=
 # learned tuning
 
 BITS = (2, 4, 8, 32)
-VARIANTS = ("PermuteMad", "Permute", "PermuteHalf", "MaskHigh")
+VARIANTS = ("PermuteMad", "Permute", "PermuteHalf", "MaskHigh")  # swar8 name suffixes
+FAMILIES = ("swar8", "scalar", "shared8")                           # name prefixes
 # Delay per unit DM of the lowest channel, in samples, for the study band
 # (1220-1520 MHz at 81.92 us); the window spread of a tile scales with it.
 STUDY_SHIFT0 = 12.1
@@ -188,13 +189,18 @@ def features(s: Shape, conf: DedispersionConf, name: str) -> np.ndarray:
     tile_d = conf.nrThreadsD1 * conf.nrItemsD1
     spread = shift0 * s.dm_step * (32 if s.subbands else 1) * tile_d
     rows = s.channels // s.subbands if s.subbands else s.channels
+    # Relative-delay growth across eight adjacent rows over the tile's DMs:
+    # how often rows share a delay vector (the shared-partial-sum family's gain).
+    share = shift0 * s.dm_step * (32 if s.subbands else 1) * tile_d * 8 / max(1, rows)
     f = [math.log2(s.channels), math.log2(rows), math.log2(max(1, s.dms)),
          math.log2(max(1, s.samples)), math.log2(s.subbands + 1), math.log2(1 + spread),
+         math.log2(1 + share),
          math.log2(conf.nrItemsD0), math.log2(conf.nrItemsD1), math.log2(conf.nrThreadsD1),
          math.log2(conf.unroll), math.log2(tile_d), math.log2(32 * conf.nrItemsD0),
          float(s.subbands > 0)]
     f += [float(s.bits == b) for b in BITS]
-    f += [float(name.endswith("_v" + str(i))) for i in range(len(VARIANTS))]
+    f += [float(name.endswith("_vkUnpack" + v)) for v in VARIANTS]
+    f += [float(name.startswith(fam)) for fam in FAMILIES]
     return np.array(f, np.float32)
 
 

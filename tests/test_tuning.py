@@ -29,6 +29,10 @@ def test_features_distinguish_configurations(engine):
     F = np.stack([tuning.features(s, k.conf, k.name) for k in ks])
     assert np.isfinite(F).all()
     assert len({tuple(r) for r in F}) == len(ks)
+    nf, nv = len(tuning.FAMILIES), len(tuning.VARIANTS)
+    for k, f in zip(ks, F):
+        assert f[-nf:].sum() == 1, k.name                      # one family
+        assert f[-nf - nv:-nf].sum() == (1 if k.name.startswith("swar8") else 0), k.name
 
 
 @pytest.mark.gpu
