@@ -33,8 +33,8 @@ __global__ void __launch_bounds__(32 * TY, (TY >= 8 ? 2 : 4))
   (void)scalar_tile<T, NS, NDT, TY, CH>(P, P.groups[g], dtile, ttile, smem, L, sc);
 }
 
-template <int NS, int NDT, int TY, int CH>
-__global__ void __launch_bounds__(32 * TY, (TY >= 8 ? 2 : 4))
+template <int NS, int NDT, int TY, int CH, int MINB>
+__global__ void __launch_bounds__(32 * TY, MINB)
     pair_kernel(const ProblemDesc P) {
   extern __shared__ __align__(128) uint8_t smem[];
   const SmemLayout L = make_layout(kFamilyPair16, P.win_samples, 32, CH, TY * NDT);
@@ -77,9 +77,9 @@ void launch_scalar(const ProblemDesc &P, unsigned grid, size_t smem,
   scalar_kernel<T, NS, NDT, TY, CH><<<grid, 32 * TY, smem, stream>>>(P);
 }
 
-template <int NS, int NDT, int TY, int CH>
+template <int NS, int NDT, int TY, int CH, int MINB>
 void launch_pair(const ProblemDesc &P, unsigned grid, size_t smem, cudaStream_t stream) {
-  pair_kernel<NS, NDT, TY, CH><<<grid, 32 * TY, smem, stream>>>(P);
+  pair_kernel<NS, NDT, TY, CH, MINB><<<grid, 32 * TY, smem, stream>>>(P);
 }
 
 template <int NW, int ND, int TY>
@@ -110,13 +110,14 @@ void launch_shared8(const ProblemDesc &P, unsigned grid, size_t smem,
    &launch_shared8<NW, ND, TY>}
 
 // Pair tiles (packed subband step two): items_t = samples per thread, items_d
-// = DMs per thread.  Not in the registry: they read only the packed
-// intermediate that a subband pipeline's own step one writes.
-#define DD_PAIR(NS, NDT, TY, CH)                                              \
-  {"pair16_i" #NS "_d" #NDT "_w" #TY "_c" #CH, kFamilyPair16, 32, NS, NDT,   \
-   TY, CH, 32 * TY, 32 * NS, TY * NDT, 0,                                     \
-   reinterpret_cast<const void *>(&pair_kernel<NS, NDT, TY, CH>),            \
-   &launch_pair<NS, NDT, TY, CH>}
+// = DMs per thread, MINB = CTAs per SM the registers are budgeted for.  Not
+// in the registry: they read only the packed intermediate that a subband
+// pipeline's own step one writes.
+#define DD_PAIR(NS, NDT, TY, CH, MINB)                                        \
+  {"pair16_i" #NS "_d" #NDT "_w" #TY "_c" #CH "_b" #MINB, kFamilyPair16, 32, \
+   NS, NDT, TY, CH, 32 * TY, 32 * NS, TY * NDT, 0,                            \
+   reinterpret_cast<const void *>(&pair_kernel<NS, NDT, TY, CH, MINB>),      \
+   &launch_pair<NS, NDT, TY, CH, MINB>}
 
 const KernelInfo *pair_kernels(int *count);
 

@@ -280,7 +280,7 @@ class LearnedTuner:
         return [candidates[i] for i in order]
 
 
-def evaluate(records, tuner: LearnedTuner, test_idx, k: int = 4, seed: int = 7) -> dict:
+def evaluate(records, tuner: LearnedTuner, test_idx, k: int = 2, seed: int = 7) -> dict:
     """Top-k by model, k random and the default configuration against the
     exhaustive best on held-out shapes; tuning wall time with and without."""
     rng = np.random.default_rng(seed)
@@ -313,7 +313,7 @@ def evaluate(records, tuner: LearnedTuner, test_idx, k: int = 4, seed: int = 7) 
             "tuning_time_ratio": t_learned / t_exhaustive if t_exhaustive else None}
 
 
-def study(count: int = 400, train_fraction: float = 0.8, steps: int = 3000, k: int = 4,
+def study(count: int = 400, train_fraction: float = 0.8, steps: int = 3000, k: int = 2,
           device: int = 0, log=print) -> dict:
     """The full learned-tuning study: sweep, train on 80 %, evaluate on 20 %."""
     shapes = study_shapes(count)
