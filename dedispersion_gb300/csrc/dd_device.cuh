@@ -845,10 +845,12 @@ __device__ __forceinline__ bool pair_tile(const ProblemDesc &P, uint32_t g,
   return true;
 }
 
-// Split a linear tile index into (group, DM tile, time tile); time fastest.
+// Split a linear tile index (offset by P.tile_base) into (group, DM tile,
+// time tile); time fastest.
 __device__ __forceinline__ void decode_tile(const ProblemDesc &P,
                                             uint32_t tile, uint32_t &g,
                                             uint32_t &dtile, uint32_t &ttile) {
+  tile += P.tile_base;
   ttile = tile % P.tiles_t;
   const uint32_t rest = tile / P.tiles_t;
   dtile = rest % P.tiles_d;
