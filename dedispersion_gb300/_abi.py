@@ -138,6 +138,9 @@ SIGNATURES = {
     "dd_filterbank_info_read": (C.c_int, [C.c_char_p, _P]),
     "dd_filterbank_read": (C.c_int, [C.c_char_p, _P, C.c_uint64, C.c_uint64, _P]),
     "dd_filterbank_observation": (C.c_int, [_P, _P]),
+    "dd_dada_info_read": (C.c_int, [C.c_char_p, _P]),
+    "dd_dada_read": (C.c_int, [C.c_char_p, _P, C.c_uint64, C.c_uint64, _P]),
+    "dd_dada_observation": (C.c_int, [_P, _P]),
     "dd_transpose_time_major": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_int, _P, C.c_uint64,
                                           C.c_uint64, _P]),
     "dd_plan_run_stats": (C.c_int, [_P, _P, _P, _P, _P]),

@@ -1,6 +1,6 @@
-// dd_ingest.cu -- SIGPROC filterbank input: header parsing, block reads and
-// the device transpose from the file's time-major samples to the engine's
-// channel rows.
+// dd_ingest.cu -- SIGPROC filterbank and PSRDADA input: header parsing,
+// block reads and the device transpose from the files' time-major samples to
+// the engine's channel rows.
 //
 // The reference reads its input through AstroData's readers (ReadData, an
 // external dependency named in its CMakeLists.txt:8-15 and absent from its
@@ -11,13 +11,24 @@
 // prefixed string; then the samples, time-major: for each time sample, for
 // each IF, nchans channel values of nbits bits, the first channel at fch1 and
 // the next ones foff MHz apart (foff < 0 in most files: descending).
+//
+// The PSRDADA file format is restated from its published definition as well:
+// an ASCII header of HDR_SIZE bytes (4096 by default), one "KEY value" per
+// line and NUL-padded, then the data.  For detected filterbank data (NPOL 1,
+// NDIM 1) in time-major order (ORDER TF or TFP) each time sample holds NCHAN
+// values of NBIT bits; the band of BW MHz (negative: channel 0 highest) is
+// centred at FREQ MHz; TSAMP is in microseconds.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <map>
+#include <sstream>
 #include <string>
 
 #include "../../include/dedisp_gb300.h"
@@ -87,6 +98,27 @@ __global__ void transpose8_kernel(const uint8_t *__restrict__ src, uint32_t coun
       dst[(uint64_t)row * row_bytes + offset + t] = tile[tx][k];
     }
   }
+}
+
+// Reads the "KEY value" lines of a PSRDADA header of `bytes` bytes.
+bool dada_keys(std::ifstream &in, uint64_t bytes, std::map<std::string, std::string> *keys) {
+  std::string text(bytes, '\0');
+  in.seekg(0);
+  if (!in.read(&text[0], (std::streamsize)bytes)) return false;
+  text.resize(std::strlen(text.c_str()));  // NUL padding ends the header
+  std::istringstream lines(text);
+  std::string line;
+  while (std::getline(lines, line)) {
+    const size_t a = line.find_first_not_of(" \t\r");
+    if (a == std::string::npos || line[a] == '#') continue;
+    const size_t b = line.find_first_of(" \t", a);
+    if (b == std::string::npos) continue;
+    const size_t c = line.find_first_not_of(" \t", b);
+    if (c == std::string::npos) continue;
+    size_t e = line.find_last_not_of(" \t\r");
+    (*keys)[line.substr(a, b - a)] = line.substr(c, e + 1 - c);
+  }
+  return true;
 }
 
 }  // namespace
@@ -187,6 +219,84 @@ dd_status dd_filterbank_observation(const dd_filterbank_info *info, dd_observati
   obs->nr_channels = info->nchans;
   obs->min_freq = (float)lowest;
   obs->channel_bandwidth = (float)std::fabs(info->foff);
+  obs->sampling_time = (float)info->tsamp;
+  return DD_OK;
+}
+
+dd_status dd_dada_info_read(const char *path, dd_dada_info *info) {
+  if (!path || !info) return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
+  std::memset(info, 0, sizeof(*info));
+  std::ifstream in(path, std::ios::binary);
+  if (!in) return fail(DD_ERR_FILE, "Impossible to open %s", path);
+  in.seekg(0, std::ios::end);
+  const uint64_t size = (uint64_t)in.tellg();
+  std::map<std::string, std::string> keys;
+  if (size < 16 || !dada_keys(in, std::min<uint64_t>(size, 4096), &keys))
+    return fail(DD_ERR_FILE, "%s: truncated PSRDADA header", path);
+  if (!keys.count("HDR_SIZE")) return fail(DD_ERR_FILE, "%s: not a PSRDADA file (no HDR_SIZE)", path);
+  const uint64_t hdr = std::strtoull(keys["HDR_SIZE"].c_str(), nullptr, 10);
+  if (hdr == 0 || hdr > size) return fail(DD_ERR_FILE, "%s: HDR_SIZE %llu past the file", path,
+                                          (unsigned long long)hdr);
+  if (hdr > 4096) {
+    keys.clear();
+    if (!dada_keys(in, hdr, &keys)) return fail(DD_ERR_FILE, "%s: truncated PSRDADA header", path);
+  }
+  for (const char *k : {"NCHAN", "NBIT", "TSAMP", "FREQ", "BW"})
+    if (!keys.count(k)) return fail(DD_ERR_FILE, "%s: PSRDADA header has no %s", path, k);
+  auto u32 = [&](const char *k, uint32_t def) {
+    return keys.count(k) ? (uint32_t)std::strtoul(keys[k].c_str(), nullptr, 10) : def;
+  };
+  info->header_bytes = hdr;
+  info->nchan = u32("NCHAN", 0);
+  info->nbit = u32("NBIT", 0);
+  info->npol = u32("NPOL", 1);
+  info->ndim = u32("NDIM", 1);
+  info->obs_offset = keys.count("OBS_OFFSET") ? std::strtoull(keys["OBS_OFFSET"].c_str(), nullptr, 10) : 0;
+  info->tsamp = std::strtod(keys["TSAMP"].c_str(), nullptr) * 1e-6;
+  info->freq = std::strtod(keys["FREQ"].c_str(), nullptr);
+  info->bw = std::strtod(keys["BW"].c_str(), nullptr);
+  if (keys.count("SOURCE"))
+    std::snprintf(info->source, sizeof(info->source), "%s", keys["SOURCE"].c_str());
+  if (keys.count("UTC_START"))
+    std::snprintf(info->utc_start, sizeof(info->utc_start), "%s", keys["UTC_START"].c_str());
+  const std::string order = keys.count("ORDER") ? keys["ORDER"] : "TF";
+  if (info->npol != 1 || info->ndim != 1 || (order != "TF" && order != "TFP"))
+    return fail(DD_ERR_UNSUPPORTED,
+                "%s: NPOL %u, NDIM %u, ORDER %s: detected time-major data only (NPOL 1, NDIM 1, "
+                "ORDER TF)", path, info->npol, info->ndim, order.c_str());
+  if (info->nchan == 0 ||
+      (info->nbit != 1 && info->nbit != 2 && info->nbit != 4 && info->nbit != 8 &&
+       info->nbit != 16 && info->nbit != 32))
+    return fail(DD_ERR_FILE, "%s: NCHAN %u, NBIT %u not supported", path, info->nchan, info->nbit);
+  const uint64_t bits_per_sample = (uint64_t)info->nchan * info->nbit;
+  if (bits_per_sample % 8) return fail(DD_ERR_FILE, "%s: a time sample is not whole bytes", path);
+  info->nsamples = (size - hdr) / (bits_per_sample / 8);
+  return DD_OK;
+}
+
+dd_status dd_dada_read(const char *path, const dd_dada_info *info, uint64_t start, uint64_t count,
+                       void *time_major) {
+  if (!path || !info || (!time_major && count)) return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (start + count > info->nsamples)
+    return fail(DD_ERR_INVALID_ARGUMENT, "samples [%llu, %llu) past the file's %llu",
+                (unsigned long long)start, (unsigned long long)(start + count),
+                (unsigned long long)info->nsamples);
+  std::ifstream in(path, std::ios::binary);
+  if (!in) return fail(DD_ERR_FILE, "Impossible to open %s", path);
+  const uint64_t sample_bytes = (uint64_t)info->nchan * info->nbit / 8;
+  in.seekg((std::streamoff)(info->header_bytes + start * sample_bytes));
+  if (!in.read(static_cast<char *>(time_major), (std::streamsize)(count * sample_bytes)))
+    return fail(DD_ERR_FILE, "%s: short read", path);
+  return DD_OK;
+}
+
+dd_status dd_dada_observation(const dd_dada_info *info, dd_observation *obs) {
+  if (!info || !obs) return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (info->bw == 0 || info->nchan == 0) return fail(DD_ERR_INVALID_ARGUMENT, "BW or NCHAN is 0");
+  const double width = std::fabs(info->bw) / info->nchan;
+  obs->nr_channels = info->nchan;
+  obs->min_freq = (float)(info->freq - std::fabs(info->bw) / 2 + 0.5 * width);
+  obs->channel_bandwidth = (float)width;
   obs->sampling_time = (float)info->tsamp;
   return DD_OK;
 }

@@ -1,14 +1,15 @@
-"""SIGPROC filterbank input (the role of AstroData's readers in the reference).
+"""SIGPROC filterbank and PSRDADA input (the role of AstroData's readers in
+the reference).
 
-    fb = Filterbank("beam.fil")
+    fb = Filterbank("beam.fil")         # or Dada("beam.dada")
     fb.observation(obs)                 # channels, frequencies, sampling time
     block = fb.read(start, count)       # [count][nchans] uint8, time-major
     fb.to_rows(d_block, d_input, row_bytes, offset)   # device transpose
 
-The header is parsed and the samples are read by the library
-(``dd_filterbank_info_read``, ``dd_filterbank_read``); ``to_rows`` transposes
-a time-major device block into a plan's channel rows on the GPU, reversing
-the channel order for files whose frequencies descend (``foff < 0``).
+The headers are parsed and the samples are read by the library
+(``dd_filterbank_*``, ``dd_dada_*``); ``to_rows`` transposes a time-major
+device block into a plan's channel rows on the GPU, reversing the channel
+order for files whose frequencies descend (``foff < 0``, ``BW < 0``).
 """
 from __future__ import annotations
 
@@ -28,11 +29,51 @@ class FilterbankInfo(C.Structure):
                 ("refdm", C.c_double), ("source_name", C.c_char * 80)]
 
 
-class Filterbank:
+class DadaInfo(C.Structure):
+    _fields_ = [("nchan", C.c_uint32), ("nbit", C.c_uint32), ("npol", C.c_uint32),
+                ("ndim", C.c_uint32), ("nsamples", C.c_uint64), ("header_bytes", C.c_uint64),
+                ("obs_offset", C.c_uint64), ("tsamp", C.c_double), ("freq", C.c_double),
+                ("bw", C.c_double), ("source", C.c_char * 64), ("utc_start", C.c_char * 32)]
+
+
+class _TimeMajorFile:
+    """Reads and device transpose shared by the two formats."""
+
+    nchans: int
+    nbits: int
+
+    def read(self, start: int, count: int) -> np.ndarray:
+        """Samples [start, start + count), time-major ([count][nchans] for
+        8-bit files; raw bytes otherwise)."""
+        nbytes = count * self.nchans * self.nbits // 8
+        buf = np.empty(nbytes, dtype=np.uint8)
+        self._read(int(start), int(count), buf.ctypes.data_as(C.c_void_p))
+        if self.nbits == 8:
+            return buf.reshape(count, self.nchans)
+        return buf
+
+    def to_rows(self, d_block, d_rows, row_bytes: int, offset: int = 0, stream=None) -> None:
+        """Device: time-major 8-bit block -> channel rows at sample ``offset``."""
+        from . import _devptr, _stream
+        if self.nbits != 8:
+            raise ValueError("the device transpose takes 8-bit samples")
+        count = int(d_block.numel()) // self.nchans if hasattr(d_block, "numel") else None
+        if count is None:
+            raise TypeError("d_block must be a device tensor")
+        check(lib().dd_transpose_time_major(C.c_void_p(_devptr(d_block)), count,
+                                            self.nchans, 1 if self.reversed else 0,
+                                            C.c_void_p(_devptr(d_rows)), int(row_bytes),
+                                            int(offset), C.c_void_p(_stream(stream))))
+
+
+class Filterbank(_TimeMajorFile):
+    """A SIGPROC filterbank file (IF 0 of multi-IF files)."""
+
     def __init__(self, path: str) -> None:
         self.path = str(path)
         self.info = FilterbankInfo()
         check(lib().dd_filterbank_info_read(self.path.encode(), C.byref(self.info)))
+        self.nchans, self.nbits = self.info.nchans, self.info.nbits
 
     @property
     def reversed(self) -> bool:
@@ -44,29 +85,48 @@ class Filterbank:
         check(lib().dd_filterbank_observation(C.byref(self.info), C.byref(obs.c)))
         return obs
 
-    def read(self, start: int, count: int) -> np.ndarray:
-        """Samples [start, start + count) of IF 0, time-major ([count][nchans]
-        for 8-bit files; raw bytes otherwise)."""
-        nbytes = count * self.info.nchans * self.info.nbits // 8
-        buf = np.empty(nbytes, dtype=np.uint8)
-        check(lib().dd_filterbank_read(self.path.encode(), C.byref(self.info), int(start),
-                                       int(count), buf.ctypes.data_as(C.c_void_p)))
-        if self.info.nbits == 8:
-            return buf.reshape(count, self.info.nchans)
-        return buf
+    def _read(self, start, count, ptr) -> None:
+        check(lib().dd_filterbank_read(self.path.encode(), C.byref(self.info), start, count, ptr))
 
-    def to_rows(self, d_block, d_rows, row_bytes: int, offset: int = 0, stream=None) -> None:
-        """Device: time-major 8-bit block -> channel rows at sample ``offset``."""
-        from . import _devptr, _stream
-        if self.info.nbits != 8:
-            raise ValueError("the device transpose takes 8-bit samples")
-        count = int(d_block.numel()) // self.info.nchans if hasattr(d_block, "numel") else None
-        if count is None:
-            raise TypeError("d_block must be a device tensor")
-        check(lib().dd_transpose_time_major(C.c_void_p(_devptr(d_block)), count,
-                                            self.info.nchans, 1 if self.reversed else 0,
-                                            C.c_void_p(_devptr(d_rows)), int(row_bytes),
-                                            int(offset), C.c_void_p(_stream(stream))))
+
+class Dada(_TimeMajorFile):
+    """A PSRDADA file of detected, time-major filterbank data."""
+
+    def __init__(self, path: str) -> None:
+        self.path = str(path)
+        self.info = DadaInfo()
+        check(lib().dd_dada_info_read(self.path.encode(), C.byref(self.info)))
+        self.nchans, self.nbits = self.info.nchan, self.info.nbit
+
+    @property
+    def reversed(self) -> bool:
+        """BW < 0: file channel 0 is the highest frequency."""
+        return self.info.bw < 0
+
+    def observation(self, obs: Observation) -> Observation:
+        check(lib().dd_dada_observation(C.byref(self.info), C.byref(obs.c)))
+        return obs
+
+    def _read(self, start, count, ptr) -> None:
+        check(lib().dd_dada_read(self.path.encode(), C.byref(self.info), start, count, ptr))
+
+
+def write_dada(path: str, data: np.ndarray, *, freq: float, bw: float, tsamp_us: float,
+               hdr_size: int = 4096, source: str = "synthetic", extra: dict | None = None) -> None:
+    """Write a PSRDADA file: data is time-major [samples][nchan] uint8 (file
+    channel order).  For tests and examples."""
+    data = np.ascontiguousarray(data, dtype=np.uint8)
+    keys = {"HDR_VERSION": "1.0", "HDR_SIZE": str(hdr_size), "NCHAN": str(data.shape[1]),
+            "NBIT": "8", "NPOL": "1", "NDIM": "1", "ORDER": "TF", "TSAMP": repr(tsamp_us),
+            "FREQ": repr(freq), "BW": repr(bw), "SOURCE": source,
+            "UTC_START": "2026-01-01-00:00:00", "OBS_OFFSET": "0"}
+    keys.update(extra or {})
+    text = "".join(f"{k:<16}{v}\n" for k, v in keys.items()).encode()
+    if len(text) > hdr_size:
+        raise ValueError("header does not fit HDR_SIZE")
+    with open(path, "wb") as f:
+        f.write(text + b"\0" * (hdr_size - len(text)))
+        f.write(data.tobytes())
 
 
 def write_filterbank(path: str, data: np.ndarray, *, fch1: float, foff: float, tsamp: float,

@@ -353,11 +353,11 @@ dd_status dd_plan_run_stats(dd_plan *plan, const void *d_input, float *d_output,
 dd_status dd_dm_stats_from_accum(const dd_dm_accum *accum, size_t rows, uint32_t samples,
                                  dd_dm_stats *stats);
 
-/* ---- ingest: SIGPROC filterbank files ------------------------------------ */
+/* ---- ingest: SIGPROC filterbank and PSRDADA files ------------------------- */
 /* The reference reads its input through AstroData's readers (ReadData, an
- * external dependency, CMakeLists.txt:8-15); this is the SIGPROC filterbank
- * path of that role, with the time-major to channel-row transpose on the
- * device. */
+ * external dependency, CMakeLists.txt:8-15); these are the SIGPROC filterbank
+ * and PSRDADA paths of that role, with the time-major to channel-row
+ * transpose on the device. */
 typedef struct dd_filterbank_info {
   uint32_t nchans, nbits, nifs, nbeams, ibeam, data_type;
   uint64_t nsamples;      /* from the header, else from the file size */
@@ -377,6 +377,29 @@ dd_status dd_filterbank_read(const char *path, const dd_filterbank_info *info,
  * from the header: the engine's channel c is at min_freq + c * bandwidth, so
  * files with foff < 0 are read with their channels reversed. */
 dd_status dd_filterbank_observation(const dd_filterbank_info *info, dd_observation *obs);
+/* A PSRDADA file: an ASCII header of HDR_SIZE bytes ("KEY value" lines),
+ * then the samples.  Detected filterbank data only: NPOL = 1, NDIM = 1,
+ * ORDER TF or TFP (time-major), NBIT 1/2/4/8/16/32. */
+typedef struct dd_dada_info {
+  uint32_t nchan, nbit, npol, ndim;
+  uint64_t nsamples;      /* from the data bytes after the header */
+  uint64_t header_bytes;  /* HDR_SIZE: offset of the first sample */
+  uint64_t obs_offset;    /* OBS_OFFSET: bytes of the observation before this file */
+  double tsamp;           /* seconds (TSAMP is in microseconds) */
+  double freq, bw;        /* MHz: centre of the band, total bandwidth (< 0: descending) */
+  char source[64];
+  char utc_start[32];
+} dd_dada_info;
+/* Parse the header of a PSRDADA file. */
+dd_status dd_dada_info_read(const char *path, dd_dada_info *info);
+/* Samples [start, start + count), time-major, into a host buffer of
+ * count * nchan * nbit / 8 bytes. */
+dd_status dd_dada_read(const char *path, const dd_dada_info *info, uint64_t start,
+                       uint64_t count, void *time_major);
+/* Channel count, lowest channel centre, channel width and sampling time of
+ * `obs` from the header (channel i of the file is centred at
+ * freq - bw / 2 + (i + 0.5) * bw / nchan; bw < 0 files are reversed). */
+dd_status dd_dada_observation(const dd_dada_info *info, dd_observation *obs);
 /* Device: a time-major 8-bit block [count][nchans] into channel rows of a
  * plan's input (row c at d_dst + c * dst_row_bytes), at sample
  * dst_sample_offset of each row; `reverse` = 1 writes file channel c to row

@@ -1,4 +1,5 @@
-"""SIGPROC filterbank ingest: header, observation mapping, reads, device transpose.
+"""SIGPROC filterbank and PSRDADA ingest: header, observation mapping, reads,
+device transpose.
 
 A file written by ``write_filterbank`` (descending frequencies, as most
 telescopes write them) must come back unchanged; its channels map onto the
@@ -78,6 +79,49 @@ def test_two_ifs_reads_the_first(tmp_path):
     np.testing.assert_array_equal(fb.read(2, 5), data[2:7, 0])
 
 
+def _dada(tmp_path, samples=500, nchan=64, seed=2, bw=-64.0, **kw):
+    rng = np.random.default_rng(seed)
+    data = rng.integers(0, 256, size=(samples, nchan), dtype=np.uint8)
+    path = tmp_path / "beam.dada"
+    ingest.write_dada(path, data, freq=1400.0, bw=bw, tsamp_us=64.0, **kw)
+    return path, data
+
+
+def test_dada_header_reads_and_observation(tmp_path):
+    path, data = _dada(tmp_path)
+    f = ingest.Dada(path)
+    assert f.info.nchan == 64 and f.info.nbit == 8 and f.info.nsamples == 500
+    assert f.info.header_bytes == 4096 and f.info.tsamp == pytest.approx(64e-6)
+    assert f.info.freq == 1400.0 and f.info.bw == -64.0 and f.reversed
+    assert f.info.source == b"synthetic"
+    np.testing.assert_array_equal(f.read(0, 500), data)
+    np.testing.assert_array_equal(f.read(77, 13), data[77:90])
+    obs = f.observation(dd.Observation())
+    # 64 channels of 1 MHz centred at 1400 MHz: the lowest centre is 1368.5
+    assert obs.getNrChannels() == 64 and obs.getMinFreq() == pytest.approx(1368.5)
+    assert obs.getChannelBandwidth() == pytest.approx(1.0)
+    with pytest.raises(dd.DedispersionError, match="past the file"):
+        f.read(490, 20)
+    # a larger header, ascending band
+    p2, d2 = _dada(tmp_path, bw=32.0, hdr_size=8192, samples=10, nchan=16)
+    g = ingest.Dada(p2)
+    assert g.info.header_bytes == 8192 and not g.reversed
+    np.testing.assert_array_equal(g.read(0, 10), d2)
+
+
+def test_dada_rejects_what_it_cannot_read(tmp_path):
+    bad = tmp_path / "bad.dada"
+    bad.write_bytes(b"NCHAN 4\nNBIT 8\n" + b"\0" * 100)
+    with pytest.raises(dd.DedispersionError, match="HDR_SIZE"):
+        ingest.Dada(bad)
+    p, _ = _dada(tmp_path, extra={"NPOL": "2"})
+    with pytest.raises(dd.DedispersionError, match="NPOL 2"):
+        ingest.Dada(p)
+    p, _ = _dada(tmp_path, extra={"ORDER": "FPT"})
+    with pytest.raises(dd.DedispersionError, match="ORDER FPT"):
+        ingest.Dada(p)
+
+
 @pytest.mark.gpu
 def test_device_transpose(gpu, tmp_path):
     torch = pytest.importorskip("torch")
@@ -128,4 +172,38 @@ def test_filterbank_to_dedispersion_matches_oracle(gpu, oracle, tmp_path):
     row = lay.output_row_elems
     np.testing.assert_array_equal(got.reshape(-1, row)[:, :2048].view(np.uint32),
                                   want.reshape(-1, row)[:, :2048].view(np.uint32))
+    p.close()
+
+
+@pytest.mark.gpu
+def test_dada_to_dedispersion_matches_oracle(gpu, oracle, tmp_path):
+    """The same dispersed pulse through a PSRDADA file (descending band)."""
+    torch = pytest.importorskip("torch")
+    obs = syn.make_observation(256, 1300.0, 0.5, 6.4e-5, 2048, 128, 0.0, 0.5, padding=128)
+    shifts = dd.getShifts(obs, 128)
+    rows = syn.make_input(obs, 8, 128, seed=6, mean=100.0, sigma=15.0, pulses=1, shifts=shifts)
+    lay = dd.layout(obs, dd.DD_SINGLE_STEP, 8, 128, shifts)
+    S_disp = obs.getNrSamplesPerDispersedBatch()
+    chan_major = rows.reshape(256, lay.input_row_bytes)[:, :S_disp]
+    # channel centres 1300 + c * 0.5 MHz: a band of 128 MHz centred at 1363.75
+    path = tmp_path / "pulse.dada"
+    ingest.write_dada(path, chan_major[::-1].T, freq=1363.75, bw=-128.0, tsamp_us=64.0)
+    f = ingest.Dada(path)
+    assert f.observation(obs.copy()).getMinFreq() == pytest.approx(1300.0)
+    d_in = torch.zeros(lay.input_bytes, dtype=torch.uint8, device="cuda")
+    f.to_rows(torch.from_numpy(f.read(0, S_disp).copy()).cuda(), d_in, lay.input_row_bytes, 0)
+    zapped = np.zeros(lay.zapped_elems, np.uint32)
+    mapping = syn.identity_mapping(obs, 128)
+    p = dd.Plan(obs, dd.DD_SINGLE_STEP, 8, 128)
+    p.setShifts(shifts)
+    p.setZappedChannels(zapped)
+    p.setBeamMapping(mapping)
+    d_out = torch.zeros(lay.output_bytes // 4, dtype=torch.float32, device="cuda")
+    p.run(d_in, d_out)
+    p.check()
+    want = np.zeros(lay.output_bytes // 4, np.float32)
+    oracle.dedispersion(obs.c, zapped, mapping, rows, want, shifts, 128, 8)
+    row = lay.output_row_elems
+    np.testing.assert_array_equal(d_out.cpu().numpy().reshape(-1, row)[:, :2048],
+                                  want.reshape(-1, row)[:, :2048])
     p.close()
