@@ -163,6 +163,7 @@ SIGNATURES = {
     "dd_stream_info": (C.c_int, [_P, _U32P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
                                  _U32P]),
     "dd_stream_push": (C.c_int, [_P, _P]),
+    "dd_stream_set_time_major": (C.c_int, [_P, C.c_int]),
     "dd_stream_destroy": (C.c_int, [_P]),
     "dd_mlp_create": (C.c_int, [C.POINTER(_P), C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64,
                                 C.c_int]),

@@ -157,6 +157,11 @@ struct dd_stream {
   cudaStream_t capture = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  // Time-major input (dd_stream_set_time_major): the staged block [S][C] is
+  // copied to d_block and transposed into the ring.
+  bool time_major = false;
+  int reverse = 0;
+  uint8_t *d_block = nullptr;
 };
 
 namespace {
@@ -172,6 +177,7 @@ void release(dd_stream *s) {
   if (s->d_out) cudaFree(s->d_out);
   if (s->h_in) cudaFreeHost(s->h_in);
   if (s->h_out) cudaFreeHost(s->h_out);
+  if (s->d_block) cudaFree(s->d_block);
 }
 
 // Bytes of the step-one intermediate: the float rows, or half as many packed
@@ -188,13 +194,41 @@ uint64_t total_bytes(const Geometry &g, int subband) {
   return b;
 }
 
+dd_status enqueue(dd_stream *s, cudaStream_t st);
+
+// (Re-)records the push as a graph.
+dd_status record(dd_stream *s) {
+  if (s->exec) cudaGraphExecDestroy(s->exec);
+  if (s->graph) cudaGraphDestroy(s->graph);
+  s->exec = nullptr;
+  s->graph = nullptr;
+  if (!s->capture) DDS_CUDA(cudaStreamCreateWithFlags(&s->capture, cudaStreamNonBlocking), "create stream");
+  DDS_CUDA(cudaStreamBeginCapture(s->capture, cudaStreamCaptureModeThreadLocal), "begin capture");
+  dd_status st = enqueue(s, s->capture);
+  cudaError_t e = cudaStreamEndCapture(s->capture, &s->graph);
+  if (st) return st;
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&s->exec, s->graph, 0);
+  if (e != cudaSuccess) return cuda_fail(e, "record stream graph");
+  return DD_OK;
+}
+
 dd_status enqueue(dd_stream *s, cudaStream_t st) {
   const Geometry &g = s->g;
   const uint32_t C = g.one.nr_channels, S = g.one.nr_samples_per_batch;
   const uint64_t tail_b = bytes_of(g.tail, s->bits), new_b = bytes_of(S, s->bits);
-  // 1. new samples after the tail
-  DDS_CUDA(cudaMemcpy2DAsync(s->d_ring + tail_b, g.ring.input_row_bytes, s->h_in, s->in_row_bytes,
-                             new_b, C, cudaMemcpyHostToDevice, st), "copy batch to ring");
+  // 1. new samples after the tail (channel rows, or a time-major block
+  //    transposed into the rows on the device)
+  if (s->time_major) {
+    DDS_CUDA(cudaMemcpyAsync(s->d_block, s->h_in, (size_t)S * C, cudaMemcpyHostToDevice, st),
+             "copy batch");
+    dd_status r = dd_transpose_time_major(s->d_block, S, C, s->reverse, s->d_ring,
+                                          g.ring.input_row_bytes, g.tail, st);
+    if (r) return r;
+  } else {
+    DDS_CUDA(cudaMemcpy2DAsync(s->d_ring + tail_b, g.ring.input_row_bytes, s->h_in,
+                               s->in_row_bytes, new_b, C, cudaMemcpyHostToDevice, st),
+             "copy batch to ring");
+  }
   // 2. dedisperse
   dd_status r = dd_plan_run(s->plan1, s->d_ring, s->subband ? s->d_mid : s->d_out, st);
   if (!r && s->subband) r = dd_plan_run(s->plan2, s->d_mid, s->d_out, st);
@@ -291,17 +325,22 @@ dd_status dd_stream_create(dd_stream **out, const dd_observation *obs, int subba
   if (e != cudaSuccess) return bail(cuda_fail(e, "allocate stream buffers"));
   std::memset(s->h_in, 0, s->in_row_bytes * C);
   s->device_bytes = total_bytes(g, s->subband);
-  // record the push
-  e = cudaStreamCreateWithFlags(&s->capture, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaStreamBeginCapture(s->capture, cudaStreamCaptureModeThreadLocal);
-  if (e != cudaSuccess) return bail(cuda_fail(e, "begin capture"));
-  st = enqueue(s, s->capture);
-  e = cudaStreamEndCapture(s->capture, &s->graph);
+  st = record(s);
   if (st) return bail(st);
-  if (e == cudaSuccess) e = cudaGraphInstantiate(&s->exec, s->graph, 0);
-  if (e != cudaSuccess) return bail(cuda_fail(e, "record stream graph"));
   *out = s;
   return DD_OK;
+}
+
+dd_status dd_stream_set_time_major(dd_stream *s, int reverse) {
+  if (!s) return fail(DD_ERR_INVALID_ARGUMENT, "stream is NULL");
+  if (s->bits != 8) return fail(DD_ERR_UNSUPPORTED, "time-major input takes 8-bit samples");
+  DDS_CUDA(cudaSetDevice(s->device), "select device");
+  const uint64_t bytes = (uint64_t)s->g.one.nr_samples_per_batch * s->g.one.nr_channels;
+  if (!s->d_block) DDS_CUDA(cudaMalloc(&s->d_block, std::max<uint64_t>(bytes, 16)), "allocate block");
+  s->time_major = true;
+  s->reverse = reverse ? 1 : 0;
+  s->device_bytes = total_bytes(s->g, s->subband) + bytes;
+  return record(s);
 }
 
 dd_status dd_stream_buffers(dd_stream *s, void **h_input, float **h_output, float **d_output) {

@@ -124,6 +124,16 @@ class Stream:
                                             ).reshape(self.output_rows, cfg.samples)
         self.dm_samples = self.output_rows * cfg.samples
 
+    def set_time_major(self, reverse: bool = False) -> None:
+        """Take batches as time-major 8-bit blocks (file order); ``staging``
+        becomes a [samples][channels] view of the same pinned buffer."""
+        check(lib().dd_stream_set_time_major(self._h, 1 if reverse else 0))
+        self.staging = self.staging.reshape(-1)[:self.cfg.samples * self.cfg.channels].reshape(
+            self.cfg.samples, self.cfg.channels)
+        tail, nbytes = C.c_uint32(0), C.c_uint64(0)
+        check(lib().dd_stream_info(self._h, C.byref(tail), C.byref(nbytes), None, None))
+        self.device_bytes = nbytes.value
+
     def push(self, cuda_stream) -> None:
         s = cuda_stream if isinstance(cuda_stream, int) else int(cuda_stream.cuda_stream)
         check(lib().dd_stream_push(self._h, C.c_void_p(s)))

@@ -472,6 +472,12 @@ dd_status dd_stream_info(const dd_stream *stream, uint32_t *tail,
  * copy the output to the pinned output, carry the tail.  Refill the staging
  * input only after the previous push completed. */
 dd_status dd_stream_push(dd_stream *stream, void *cuda_stream);
+/* From now on take each batch as a time-major 8-bit block [S][C] in the
+ * staging input (file order of SIGPROC and PSRDADA data; `reverse` = 1 when
+ * the file's channel 0 is the highest frequency): a push copies the block to
+ * the device and transposes it into the ring (dd_transpose_time_major).
+ * Adds S * C device bytes.  8-bit streams only. */
+dd_status dd_stream_set_time_major(dd_stream *stream, int reverse);
 dd_status dd_stream_destroy(dd_stream *stream);
 
 /* ---- learned tuning: the cost model's network ---------------------------- */

@@ -121,3 +121,27 @@ def test_served_batches_equal_plain_path(gpu):
             assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (cfg.name, k)
             prev = window[:, window.shape[1] - tail_b:] if tail_b else prev
     server.close()
+
+
+@pytest.mark.gpu
+def test_time_major_input_equals_channel_rows(gpu):
+    """A stream fed file-order blocks (time-major, channels descending) gives
+    the same outputs as one fed channel rows, single step and subband."""
+    torch = pytest.importorskip("torch")
+    cs = torch.cuda.Stream()
+    for cfg in [c for c in small_beams() if c.bits == 8][:2]:
+        a, b = serving.Stream(cfg), serving.Stream(cfg)
+        nb = b.device_bytes
+        b.set_time_major(reverse=True)
+        assert b.device_bytes == nb + cfg.samples * cfg.channels
+        assert b.staging.shape == (cfg.samples, cfg.channels)
+        for k in range(3):
+            data = batch_data(cfg, k)
+            a.staging[:, :cfg.samples] = data
+            b.staging[:] = data[::-1].T
+            a.push(cs)
+            b.push(cs)
+            cs.synchronize()
+            assert np.array_equal(a.output.view(np.uint32), b.output.view(np.uint32)), (cfg.name, k)
+        a.close()
+        b.close()
