@@ -301,6 +301,7 @@ struct dd_plan {
   // step two (a pair tile) reads it; set by a subband pipeline only.
   bool packed = false;
   uint32_t flush_rows = 0;  // step two: rows per 16-bit lane flush
+  uint32_t max_delay = 0;   // largest row delay of the built tables
 };
 
 namespace {
@@ -416,6 +417,7 @@ dd_status rebuild(dd_plan *p) {
     return fail(DD_ERR_INVALID_ARGUMENT,
                 "rows hold %u samples but %u output samples + max delay %u are needed",
                 d.row_samples, d.nr_samples, max_delay);
+  p->max_delay = max_delay;
   int dev_max = 0, sm_max = 0;
   {
     DeviceGuard g(p->device);
@@ -1193,9 +1195,10 @@ struct SyncCache {
   float *d_out = nullptr;
   size_t cap_in = 0, cap_out = 0;
   cudaStream_t stream = nullptr;
-  // Chunked runs: a second compute stream, the output copy stream, and
-  // [input ready, chunk 0 .. kChunks - 1 done, copies done, side done].
-  cudaStream_t side = nullptr, copy = nullptr;
+  // Chunked runs: a second compute stream, the output and input copy
+  // streams, and events [input of chunk 0 .. kChunks - 1, chunk 0 ..
+  // kChunks - 1 done, copies done, side done].
+  cudaStream_t side = nullptr, copy = nullptr, copy_in = nullptr;
   std::vector<cudaEvent_t> events;
   ~SyncCache() {
     if (plan) dd_plan_destroy(plan);
@@ -1204,6 +1207,7 @@ struct SyncCache {
     if (stream) cudaStreamDestroy(stream);
     if (side) cudaStreamDestroy(side);
     if (copy) cudaStreamDestroy(copy);
+    if (copy_in) cudaStreamDestroy(copy_in);
     for (cudaEvent_t e : events) cudaEventDestroy(e);
   }
 };
@@ -1278,15 +1282,14 @@ dd_status run_sync(const dd_observation *o, dd_mode mode, const uint32_t *zapped
     DD_CUDA(cudaMalloc(&c.d_out, out_bytes), "allocate device output");
     c.cap_out = out_bytes;
   }
-  if (in_bytes)
-    DD_CUDA(cudaMemcpyAsync(c.d_in, input, in_bytes, cudaMemcpyHostToDevice, c.stream), "copy input");
   const dd_plan *p = c.plan;
-  const uint64_t gd_total = (uint64_t)p->nr_groups * p->tiles_d;
-  const uint64_t tiles = gd_total * p->tiles_t;
-  // Output rows are contiguous in tile order except in step one (its DM rows
-  // interleave subbands): there, and for small problems, one launch and one
-  // copy.
-  if (mode == DD_STEP_ONE || tiles < kChunkMinTiles || gd_total < 2 || !d.nr_samples) {
+  const uint64_t tt_total = p->tiles_t;
+  const uint64_t tiles = (uint64_t)p->nr_groups * p->tiles_d * tt_total;
+  if (tiles < kChunkMinTiles || tt_total < 2 || !d.nr_samples || !d.output_rows) {
+    // Small problems: one copy in, one launch, one copy out.
+    if (in_bytes)
+      DD_CUDA(cudaMemcpyAsync(c.d_in, input, in_bytes, cudaMemcpyHostToDevice, c.stream),
+              "copy input");
     st = dd_plan_run(c.plan, c.d_in, c.d_out, c.stream);
     if (st) return st;
     if (d.output_rows && d.nr_samples)
@@ -1296,12 +1299,16 @@ dd_status run_sync(const dd_observation *o, dd_mode mode, const uint32_t *zapped
               "copy output");
     return dd_plan_check(c.plan, c.stream);
   }
-  // Chunked: the DM tiles in kChunks launches alternating between two
-  // streams (a chunk's last partial wave overlaps the next chunk), each
-  // chunk's finished rows copied to the host while later chunks compute.
-  if (!c.side) DD_CUDA(cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking), "create stream");
-  if (!c.copy) DD_CUDA(cudaStreamCreateWithFlags(&c.copy, cudaStreamNonBlocking), "create stream");
-  while (c.events.size() < kChunks + 3) {
+  // Chunked over time tiles: chunk k computes every (group, DM tile) over
+  // its time tiles, so it needs input samples below its last tile's end +
+  // the largest delay.  The input comes in pieces on a copy stream, each
+  // before the first chunk that reads it; chunks alternate between two
+  // compute streams (a chunk's last partial wave overlaps the next one); each
+  // chunk's output columns go back on a third stream while later chunks
+  // compute.
+  for (cudaStream_t *x : {&c.side, &c.copy, &c.copy_in})
+    if (!*x) DD_CUDA(cudaStreamCreateWithFlags(x, cudaStreamNonBlocking), "create stream");
+  while (c.events.size() < 2 * kChunks + 2) {
     cudaEvent_t e;
     DD_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "create event");
     c.events.push_back(e);
@@ -1309,38 +1316,53 @@ dd_status run_sync(const dd_observation *o, dd_mode mode, const uint32_t *zapped
   dd::ProblemDesc P{};
   st = dd::plan_problem(p, c.d_in, c.d_out, &P, nullptr);
   if (st) return st;
-  DD_CUDA(cudaEventRecord(c.events[0], c.stream), "record input");
-  DD_CUDA(cudaStreamWaitEvent(c.side, c.events[0], 0), "wait input");
-  const uint32_t K = (uint32_t)std::min<uint64_t>(kChunks, gd_total);
-  const uint64_t D = d.nr_dms, tile_d = (uint64_t)p->kinfo->tile_d;
-  auto rows_before = [&](uint64_t gd) {  // output rows of the first gd (group, DM tile)
-    return gd / p->tiles_d * D + std::min<uint64_t>(gd % p->tiles_d * tile_d, D);
+  const uint32_t K = (uint32_t)std::min<uint64_t>(kChunks, tt_total);
+  const uint64_t T = (uint64_t)p->kinfo->tile_t;
+  const uint64_t in_rows = d.input_bytes / d.row_bytes;
+  const uint64_t elem_bits = mode == DD_STEP_TWO ? 32 : bits;
+  // Bytes of each input row that hold samples below `samples`, with slack
+  // for the staged windows' alignment.
+  auto row_bytes_below = [&](uint64_t samples) {
+    const uint64_t bytes = (samples * elem_bits + 7) / 8 + 128;
+    return std::min<uint64_t>((bytes + 15) / 16 * 16, d.row_bytes);
   };
-  // Every launch first, then the copies: a copy to pageable host memory
-  // blocks this thread, and the later chunks must already be queued.
+  const uint8_t *in8 = static_cast<const uint8_t *>(input);
+  uint8_t *din8 = static_cast<uint8_t *>(c.d_in);
+  uint64_t copied = 0;
   for (uint32_t k = 0; k < K; k++) {
-    const uint64_t a = gd_total * k / K, b = gd_total * (k + 1) / K;
+    const uint64_t a = tt_total * k / K, b = tt_total * (k + 1) / K;
+    const uint64_t need = k + 1 == K ? d.row_bytes : row_bytes_below(b * T + p->max_delay);
+    if (need > copied) {
+      DD_CUDA(cudaMemcpy2DAsync(din8 + copied, d.row_bytes, in8 + copied, d.row_bytes,
+                                need - copied, in_rows, cudaMemcpyHostToDevice, c.copy_in),
+              "copy input");
+      copied = need;
+    }
+    DD_CUDA(cudaEventRecord(c.events[k], c.copy_in), "record input");
     cudaStream_t sk = (k & 1u) ? c.side : c.stream;
-    P.tile_base = (uint32_t)(a * p->tiles_t);
-    p->kinfo->launch(P, (unsigned)((b - a) * p->tiles_t), p->smem, sk);
+    DD_CUDA(cudaStreamWaitEvent(sk, c.events[k], 0), "wait input");
+    P.ttile_base = (uint32_t)a;
+    P.ttile_count = (uint32_t)(b - a);
+    p->kinfo->launch(P, (unsigned)((uint64_t)p->nr_groups * p->tiles_d * (b - a)), p->smem, sk);
     DD_CUDA(cudaGetLastError(), "launch dedispersion kernel");
-    DD_CUDA(cudaEventRecord(c.events[1 + k], sk), "record chunk");
+    DD_CUDA(cudaEventRecord(c.events[kChunks + k], sk), "record chunk");
   }
+  // The copies out after every launch: a copy to pageable host memory blocks
+  // this thread, and the later chunks must already be queued.
   for (uint32_t k = 0; k < K; k++) {
-    const uint64_t a = gd_total * k / K, b = gd_total * (k + 1) / K;
-    DD_CUDA(cudaStreamWaitEvent(c.copy, c.events[1 + k], 0), "wait chunk");
-    const uint64_t r0 = rows_before(a), r1 = rows_before(b);
-    if (r1 > r0)
-      DD_CUDA(cudaMemcpy2DAsync(output + r0 * d.out_row, d.out_row * sizeof(float),
-                                c.d_out + r0 * d.out_row, d.out_row * sizeof(float),
-                                (size_t)d.nr_samples * sizeof(float), r1 - r0,
-                                cudaMemcpyDeviceToHost, c.copy),
+    const uint64_t a = tt_total * k / K, b = tt_total * (k + 1) / K;
+    const uint64_t t0 = a * T, t1 = std::min<uint64_t>(b * T, d.nr_samples);
+    DD_CUDA(cudaStreamWaitEvent(c.copy, c.events[kChunks + k], 0), "wait chunk");
+    if (t1 > t0)
+      DD_CUDA(cudaMemcpy2DAsync(output + t0, d.out_row * sizeof(float), c.d_out + t0,
+                                d.out_row * sizeof(float), (t1 - t0) * sizeof(float),
+                                d.output_rows, cudaMemcpyDeviceToHost, c.copy),
               "copy output");
   }
-  DD_CUDA(cudaEventRecord(c.events[K + 1], c.copy), "record copies");
-  DD_CUDA(cudaEventRecord(c.events[K + 2], c.side), "record side");
-  DD_CUDA(cudaStreamWaitEvent(c.stream, c.events[K + 1], 0), "join copies");
-  DD_CUDA(cudaStreamWaitEvent(c.stream, c.events[K + 2], 0), "join side");
+  DD_CUDA(cudaEventRecord(c.events[2 * kChunks], c.copy), "record copies");
+  DD_CUDA(cudaEventRecord(c.events[2 * kChunks + 1], c.side), "record side");
+  DD_CUDA(cudaStreamWaitEvent(c.stream, c.events[2 * kChunks], 0), "join copies");
+  DD_CUDA(cudaStreamWaitEvent(c.stream, c.events[2 * kChunks + 1], 0), "join side");
   return dd_plan_check(c.plan, c.stream);
 }
 

@@ -846,13 +846,15 @@ __device__ __forceinline__ bool pair_tile(const ProblemDesc &P, uint32_t g,
 }
 
 // Split a linear tile index (offset by P.tile_base) into (group, DM tile,
-// time tile); time fastest.
+// time tile); time fastest, over P.ttile_count time tiles from P.ttile_base
+// when ttile_count is set.
 __device__ __forceinline__ void decode_tile(const ProblemDesc &P,
                                             uint32_t tile, uint32_t &g,
                                             uint32_t &dtile, uint32_t &ttile) {
   tile += P.tile_base;
-  ttile = tile % P.tiles_t;
-  const uint32_t rest = tile / P.tiles_t;
+  const uint32_t nt = P.ttile_count ? P.ttile_count : P.tiles_t;
+  ttile = tile % nt + P.ttile_base;
+  const uint32_t rest = tile / nt;
   dtile = rest % P.tiles_d;
   g = rest / P.tiles_d;
 }

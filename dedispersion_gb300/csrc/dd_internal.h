@@ -113,9 +113,12 @@ struct ProblemDesc {
   // kernel (step two) reads those rows: group (synthesized beam, p) writes
   // DM rows d of coarse DM 2p at out_offset + d * out_dm_stride and of coarse
   // DM 2p + 1 pair_stride floats further on.
-  // First tile of a launch: a launch of G CTAs computes tiles [tile_base,
-  // tile_base + G) of the problem's (group, DM tile, time tile) order.
+  // Tiles of a launch.  With ttile_count = 0 a launch of G CTAs computes
+  // tiles [tile_base, tile_base + G) of the problem's (group, DM tile, time
+  // tile) order.  With ttile_count > 0 it computes, for every (group, DM
+  // tile), the time tiles [ttile_base, ttile_base + ttile_count).
   uint32_t tile_base;
+  uint32_t ttile_base, ttile_count;
   uint32_t packed;
   uint32_t pair_groups;   // pairs of coarse DMs (groups per synthesized beam)
   uint32_t pair_d1;       // coarse DMs
