@@ -1179,8 +1179,9 @@ namespace {
 // calls, so that repeated calls on one geometry only copy and launch.
 // Chunked host-buffer runs (run_sync): launches per call and the smallest
 // problem (in tiles) that is split.  At 1536 channels x 2048 DMs x 24576
-// samples a call takes 4.17 ms in one launch and 3.67 / 3.42 / 3.28 / 3.39 ms
-// in 4 / 8 / 16 / 32 chunks (one GB300, pinned host buffers).
+// samples a call takes 4.19 ms in one chunk and 3.27 / 3.13 / 3.08 / 3.06 /
+// 3.06 / 3.24 ms in 4 / 8 / 12 / 16 / 24 / 32 (one GB300, pinned host
+// buffers; the kernel alone takes 2.87 ms).
 constexpr uint32_t kChunks = 16;
 constexpr uint64_t kChunkMinTiles = 2048;
 
