@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <cstdarg>
 #include <cstdio>
+#include <cstring>
 #include <vector>
 
 #include "../../include/dedisp_gb300.h"
@@ -161,6 +162,27 @@ dd_status build(dd_subband *s) {
   return DD_OK;
 }
 
+// Per-thread state of the synchronous host-buffer call.
+struct HostCache {
+  dd_subband *pipe = nullptr;
+  dd_observation obs{};
+  uint32_t bits = 0, padding = 0;
+  void *d_in = nullptr, *d_out = nullptr;
+  uint64_t cap_in = 0, cap_out = 0;
+  cudaStream_t stream = nullptr;
+  void reset() {
+    if (pipe) dd_subband_destroy(pipe);
+    pipe = nullptr;
+  }
+  ~HostCache() {
+    reset();
+    if (d_in) cudaFree(d_in);
+    if (d_out) cudaFree(d_out);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+thread_local HostCache g_host;
+
 }  // namespace
 
 extern "C" {
@@ -265,34 +287,57 @@ dd_status dd_subband_dedispersion(const dd_observation *obs, const uint32_t *zap
   dd_status st = dd_get_layout(obs, DD_STEP_ONE, input_bits, padding, nullptr, &l1);
   if (!st) st = dd_get_layout(obs, DD_STEP_TWO, 32, padding, nullptr, &l2);
   if (st) return st;
-  dd_subband *s = nullptr;
-  st = dd_subband_create(&s, obs, input_bits, padding, 0);
+  // One pipeline and buffers per thread, rebuilt when the geometry or a
+  // table changes (repeated calls on the same observation build once).
+  HostCache &c = g_host;
+  const size_t n_map = (size_t)obs->nr_synthesized_beams * l2.mapping_row_elems;
+  const bool same = c.pipe && c.bits == input_bits && c.padding == padding &&
+                    std::memcmp(&c.obs, obs, sizeof(*obs)) == 0;
+  if (!same) {
+    c.reset();
+    st = dd_subband_create(&c.pipe, obs, input_bits, padding, 0);
+    if (st) return st;
+    c.obs = *obs;
+    c.bits = input_bits;
+    c.padding = padding;
+  }
+  const bool tables = same && c.pipe->shifts.size() == l1.shifts_elems &&
+                      std::memcmp(c.pipe->shifts.data(), shifts, l1.shifts_elems * 4) == 0 &&
+                      c.pipe->shifts2.size() == l2.shifts_elems &&
+                      std::memcmp(c.pipe->shifts2.data(), shifts_step_two, l2.shifts_elems * 4) == 0 &&
+                      c.pipe->zapped.size() == l1.zapped_elems &&
+                      std::memcmp(c.pipe->zapped.data(), zapped, l1.zapped_elems * 4) == 0 &&
+                      c.pipe->mapping.size() == n_map &&
+                      std::memcmp(c.pipe->mapping.data(), beam_mapping, n_map * 4) == 0;
+  if (!tables) {
+    st = dd_subband_set_tables(c.pipe, shifts, l1.shifts_elems, shifts_step_two, l2.shifts_elems,
+                               zapped, l1.zapped_elems, beam_mapping, n_map);
+    if (st) return st;
+  }
+  DDS_CUDA(cudaSetDevice(0), "select device");
+  if (!c.stream) DDS_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking), "create stream");
+  if (l1.input_bytes > c.cap_in) {
+    if (c.d_in) cudaFree(c.d_in);
+    c.d_in = nullptr;
+    c.cap_in = 0;
+    DDS_CUDA(cudaMalloc(&c.d_in, std::max<uint64_t>(l1.input_bytes, 16)), "allocate input");
+    c.cap_in = l1.input_bytes;
+  }
+  if (l2.output_bytes > c.cap_out) {
+    if (c.d_out) cudaFree(c.d_out);
+    c.d_out = nullptr;
+    c.cap_out = 0;
+    DDS_CUDA(cudaMalloc(&c.d_out, std::max<uint64_t>(l2.output_bytes, 16)), "allocate output");
+    c.cap_out = l2.output_bytes;
+  }
+  DDS_CUDA(cudaMemcpyAsync(c.d_in, input, l1.input_bytes, cudaMemcpyHostToDevice, c.stream),
+           "copy input");
+  DDS_CUDA(cudaMemsetAsync(c.d_out, 0, l2.output_bytes, c.stream), "clear output");
+  st = dd_subband_run(c.pipe, c.d_in, static_cast<float *>(c.d_out), c.stream);
   if (st) return st;
-  void *d_in = nullptr, *d_out = nullptr;
-  cudaStream_t stream = nullptr;
-  auto done = [&](dd_status code) {
-    if (d_in) cudaFree(d_in);
-    if (d_out) cudaFree(d_out);
-    if (stream) cudaStreamDestroy(stream);
-    dd_subband_destroy(s);
-    return code;
-  };
-  st = dd_subband_set_tables(s, shifts, l1.shifts_elems, shifts_step_two, l2.shifts_elems, zapped,
-                             l1.zapped_elems, beam_mapping,
-                             (size_t)obs->nr_synthesized_beams * l2.mapping_row_elems);
-  if (st) return done(st);
-  cudaError_t e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaMalloc(&d_in, std::max<uint64_t>(l1.input_bytes, 16));
-  if (e == cudaSuccess) e = cudaMalloc(&d_out, std::max<uint64_t>(l2.output_bytes, 16));
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(d_in, input, l1.input_bytes, cudaMemcpyHostToDevice, stream);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d_out, 0, l2.output_bytes, stream);
-  if (e != cudaSuccess) return done(cuda_fail(e, "stage subband buffers"));
-  st = dd_subband_run(s, d_in, static_cast<float *>(d_out), stream);
-  if (st) return done(st);
-  e = cudaMemcpyAsync(output, d_out, l2.output_bytes, cudaMemcpyDeviceToHost, stream);
-  if (e != cudaSuccess) return done(cuda_fail(e, "copy output"));
-  return done(dd_subband_check(s, stream));
+  DDS_CUDA(cudaMemcpyAsync(output, c.d_out, l2.output_bytes, cudaMemcpyDeviceToHost, c.stream),
+           "copy output");
+  return dd_subband_check(c.pipe, c.stream);
 }
 
 }  // extern "C"

@@ -108,13 +108,18 @@ def test_float_intermediate_when_sums_can_exceed_16_bits(gpu, oracle, bits, kw):
 
 
 def test_host_call_matches_oracle_chain(gpu, oracle):
+    """The host-buffer call, three times: its cached pipeline is reused, then
+    rebuilt when the zapped mask changes."""
     obs, shifts, shifts2, zapped, inp, mapping = _case(bits=8, padding=64, seed=8, D1=6)
-    want = _oracle_chain(oracle, obs, shifts, shifts2, zapped, inp, mapping, 64, 8)
-    out = np.full(dd.layout(obs, dd.DD_STEP_TWO, 32, 64).output_bytes // 4, -1.0, np.float32)
-    dd.subbandDedispersion(obs, zapped, mapping, inp, out, shifts, shifts2, 64, 8)
     row = dd.layout(obs, dd.DD_STEP_TWO, 32, 64).output_row_elems
     S = obs.getNrSamplesPerBatch()
-    np.testing.assert_array_equal(out.reshape(-1, row)[:, :S], want.reshape(-1, row)[:, :S])
+    zapped2 = zapped.copy()
+    zapped2[:7] = 1
+    for z in (zapped, zapped, zapped2):
+        want = _oracle_chain(oracle, obs, shifts, shifts2, z, inp, mapping, 64, 8)
+        out = np.full(dd.layout(obs, dd.DD_STEP_TWO, 32, 64).output_bytes // 4, -1.0, np.float32)
+        dd.subbandDedispersion(obs, z, mapping, inp, out, shifts, shifts2, 64, 8)
+        np.testing.assert_array_equal(out.reshape(-1, row)[:, :S], want.reshape(-1, row)[:, :S])
 
 
 def test_full_shape_equals_float_steps(gpu):
