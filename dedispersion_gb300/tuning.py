@@ -13,11 +13,16 @@ cost model that times only its top candidates.
 * :class:`LearnedTuner` predicts log(time per DM-sample) of every configuration
   from shape and configuration features with the library's CUDA MLP
   (dedispersion_gb300.costmodel), then times only the top k.  The sweep stays
-  the judge; the model never touches outputs.
+  the judge; the model never touches outputs.  A trained model is saved and
+  loaded (``LearnedTuner.save`` / ``load``); on the command line
+  ``-train_model model.npz`` sweeps the seeded study shapes and saves one, and
+  ``-learned model.npz -top_k k`` times only the model's top k of a problem
+  (single step and step one; step two keeps the full sweep).
 """
 from __future__ import annotations
 
 import argparse
+import json
 import math
 import sys
 import time
@@ -146,6 +151,7 @@ class Shape:
     subbands: int
     dm_step: float = 0.2
     seed: int = 0
+    shift0: float = 0.0  # delay per unit DM of the lowest channel (0: the study band's)
 
     def mode(self) -> int:
         return DD_STEP_ONE if self.subbands else DD_SINGLE_STEP
@@ -183,9 +189,16 @@ def measured_observation(s: Shape, padding: int, max_dms: int = 256, max_samples
                                 s.dm_step, padding=padding)
 
 
+FEATURE_NAMES = ("log2 channels", "log2 rows", "log2 dms", "log2 samples", "log2 subbands+1",
+                 "log2 spread", "log2 sharing", "log2 items d0", "log2 items d1",
+                 "log2 warps d1", "log2 unroll", "log2 tile dms", "log2 tile samples",
+                 "subband") + tuple(f"bits {b}" for b in BITS) + \
+    tuple(f"variant {v}" for v in VARIANTS) + tuple(f"family {f}" for f in FAMILIES)
+
+
 def features(s: Shape, conf: DedispersionConf, name: str) -> np.ndarray:
     """Shape and configuration features of one (problem, configuration) pair."""
-    shift0 = STUDY_SHIFT0
+    shift0 = s.shift0 or STUDY_SHIFT0
     tile_d = conf.nrThreadsD1 * conf.nrItemsD1
     spread = shift0 * s.dm_step * (32 if s.subbands else 1) * tile_d
     rows = s.channels // s.subbands if s.subbands else s.channels
@@ -279,6 +292,51 @@ class LearnedTuner:
         order = np.argsort(self.predict(X))
         return [candidates[i] for i in order]
 
+    def save(self, path: str) -> None:
+        """Weights and normalisation, to rank new shapes without retraining."""
+        np.savez(path, params=self.model.params(), mu=self.mu, sd=self.sd,
+                 ymu=self.ymu, ysd=self.ysd, hidden=self.hidden, layers=self.layers,
+                 features=len(self.mu), feature_names=np.array(FEATURE_NAMES))
+
+    @classmethod
+    def load(cls, path: str, device: int = 0) -> "LearnedTuner":
+        from .costmodel import MLP
+        z = np.load(path)
+        if list(z["feature_names"]) != list(FEATURE_NAMES):
+            raise ValueError(f"{path} was trained on other features; retrain it")
+        t = cls(hidden=int(z["hidden"]), layers=int(z["layers"]), device=device)
+        t.mu, t.sd = z["mu"], z["sd"]
+        t.ymu, t.ysd = float(z["ymu"]), float(z["ysd"])
+        t.model = MLP(int(z["features"]), t.hidden, t.layers, 0, device)
+        t.model.set_params(z["params"])
+        return t
+
+
+def observation_shape(obs, mode: int, bits: int, shifts) -> Shape:
+    """The learned tuner's view of a single-step or step-one problem."""
+    shift0 = float(np.asarray(shifts)[0])
+    if mode == DD_STEP_ONE:
+        # the study's subband shapes take coarse steps of 32 fine ones
+        return Shape(channels=obs.getNrChannels(), dms=obs.getNrDMs(True) * 32,
+                     samples=obs.getNrSamplesPerBatch(True), bits=bits,
+                     subbands=obs.getNrSubbands(), dm_step=obs.getDMStep(True) / 32,
+                     shift0=shift0)
+    return Shape(channels=obs.getNrChannels(), dms=obs.getNrDMs(),
+                 samples=obs.getNrSamplesPerBatch(), bits=bits, subbands=0,
+                 dm_step=obs.getDMStep(), shift0=shift0)
+
+
+def train_model(path: str, count: int = 400, steps: int = 3000, device: int = 0,
+                log=None) -> dict:
+    """Sweep `count` seeded study shapes, train the cost model on all of them
+    and save it (LearnedTuner.load reads it back)."""
+    records = collect(study_shapes(count), device=device, log=log)
+    X, y, _ = dataset(records)
+    tuner = LearnedTuner(device=device)
+    loss = tuner.fit(X, y, steps=steps)
+    tuner.save(path)
+    return {"shapes": count, "rows": int(len(y)), "train_loss_normalised": loss, "path": path}
+
 
 def evaluate(records, tuner: LearnedTuner, test_idx, k: int = 2, seed: int = 7) -> dict:
     """Top-k by model, k random and the default configuration against the
@@ -366,11 +424,20 @@ def _args(argv):
     ap.add_argument("-zapped_channels")
     ap.add_argument("-device_name", default="GB300")
     ap.add_argument("-tuned_file")
+    # learned tuning (no reference counterpart): rank with a saved cost model
+    # and time only its top k; or train and save one
+    ap.add_argument("-learned")
+    ap.add_argument("-top_k", type=int, default=2)
+    ap.add_argument("-train_model")
+    ap.add_argument("-study_shapes", type=int, default=400)
     return ap.parse_args(argv)
 
 
 def main(argv=None) -> int:
     a = _args(argv if argv is not None else sys.argv[1:])
+    if a.train_model:
+        print(json.dumps(train_model(a.train_model, count=a.study_shapes)))
+        return 0
     if a.single_step + a.step_one + a.step_two != 1:
         print("Mutually exclusive modes, select one: -single_step -step_one -step_two",
               file=sys.stderr)
@@ -427,6 +494,12 @@ def main(argv=None) -> int:
         if a.max_unroll and c.unroll > a.max_unroll:
             continue
         cands.append(k)
+    if a.learned and not a.step_two:
+        # time only the cost model's top k (step two has no model: full sweep)
+        tuner = LearnedTuner.load(a.learned)
+        n = len(cands)
+        cands = tuner.rank(observation_shape(o, mode, bits, shifts), cands)[:max(1, a.top_k)]
+        print(f"learned: timed {len(cands)} of {n} configurations", file=sys.stderr)
     res = sweep(o, mode, bits, padding, shifts2 if a.step_two else shifts,
                 zapped if not a.step_two else None, None, iterations=a.iterations or 3,
                 candidates=cands)

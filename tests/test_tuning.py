@@ -52,7 +52,7 @@ def test_exhaustive_cli_best_line(gpu, tmp_path):
 
 
 @pytest.mark.gpu
-def test_learned_tuner_beats_random_choice(gpu):
+def test_learned_tuner_beats_random_choice(gpu, tmp_path):
     shapes = tuning.study_shapes(48, seed=99)
     # small problems keep the sweep short
     old = tuning.measured_observation
@@ -70,3 +70,21 @@ def test_learned_tuner_beats_random_choice(gpu):
     assert rep["top_k_vs_best_mean"] >= rep["random_k_vs_best_mean"]
     assert rep["top_k_vs_best_mean"] > 0.8
     assert rep["tuning_time_ratio"] < 0.5
+    # a saved model ranks the same after loading
+    path = tmp_path / "model.npz"
+    t.save(str(path))
+    u = tuning.LearnedTuner.load(str(path))
+    np.testing.assert_allclose(u.predict(X[:50]), t.predict(X[:50]), rtol=1e-6, atol=1e-6)
+    # the CLI times only the model's top 2 and prints a tuned-conf line
+    tuned = tmp_path / "tuned.conf"
+    args = [sys.executable, "-m", "dedispersion_gb300.tuning", "-iterations", "2", "-single_step",
+            "-padding", "128", "-beams", "1", "-synthesized_beams", "1", "-samples", "4096",
+            "-sampling_time", "0.00008192", "-min_freq", "1220", "-channel_bandwidth", "0.5",
+            "-channels", "256", "-dms", "128", "-dm_first", "0", "-dm_step", "0.2", "-best",
+            "-learned", str(path), "-top_k", "2", "-tuned_file", str(tuned)]
+    p = subprocess.run(args, cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert p.returncode == 0, p.stderr
+    fields = p.stdout.split()
+    assert fields[0] == "128" and len(fields) == 10
+    assert "learned: timed 2 of" in p.stderr, p.stderr
+    assert dd.readTunedDedispersionConf(str(tuned), "GB300", 128).print() == " ".join(fields[1:])
