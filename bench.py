@@ -344,7 +344,7 @@ def bench_subband(torch, device: int, steps: int, hbm_peak: float, peak_adds: fl
                     "HBM; the part that stays in L2 makes the true traffic lower"}
 
 
-def bench_batched(torch, device: int, reps: int = 3, count: int = 40):
+def bench_batched(torch, device: int, reps: int = 3, count: int = 40, peak_adds: float = 0.0):
     """40 uneven beams (384/1536 ch, 8192-32768 samples, 512-4096 DMs, steps
     0.1-0.5, 2/4/8-bit uniform input) in one CUDA graph launch (the beams'
     kernels forked over concurrent branches), against the same beams launched
@@ -355,7 +355,7 @@ def bench_batched(torch, device: int, reps: int = 3, count: int = 40):
     shapes = syn.batched_shapes(count)
     batch = dd.Batch(device)
     beams = []
-    units = 0
+    units = adds = 0
     for sh in shapes:
         obs = syn.shape_observation(sh, padding)
         shifts = dd.getShifts(obs, padding)
@@ -372,6 +372,7 @@ def bench_batched(torch, device: int, reps: int = 3, count: int = 40):
         plan.setBeamMapping(mapping)
         beams.append((obs, lay, d_in, d_out, d_ref, plan))
         units += obs.getNrDMs() * obs.getNrSamplesPerBatch()
+        adds += obs.getNrDMs() * obs.getNrSamplesPerBatch() * int((zapped[:sh["channels"]] == 0).sum())
     batch.commit()
     stream = torch.cuda.current_stream()
     batch.run(stream)
@@ -405,6 +406,8 @@ def bench_batched(torch, device: int, reps: int = 3, count: int = 40):
     return {"value": units / t_batch, "unit": UNIT, "ms_per_batch": t_batch * 1e3,
             "plain_sequential_value": units / t_plain, "plain_sequential_ms": t_plain * 1e3,
             "speedup_vs_plain": t_plain / t_batch, "beams": count, "tiles": info["tiles"],
+            "adds_per_batch": adds,
+            "adds_frac": adds / t_batch / peak_adds if peak_adds else None,
             ("branches" if shared else "persistent_ctas"): info["grid"],
             "tile": info.get("tile"), "bit_exact_vs_plain": exact,
             "launch": ("one CUDA graph: the beams' kernels on concurrent branches" if shared
@@ -586,7 +589,7 @@ def main():
     detect = bench_detect(torch, plan, d_in, d_out, stream, D, S, args.steps)
     ingest_line = bench_ingest(torch, inp, lay, obs, stream)
     subband = bench_subband(torch, local, max(10, min(args.steps, 50)), hbm_peak, peak_adds)
-    batched = bench_batched(torch, local) if not args.no_batched else None
+    batched = bench_batched(torch, local, peak_adds=peak_adds) if not args.no_batched else None
     served = bench_served(local) if not args.no_served else None
 
     if rank != 0:
