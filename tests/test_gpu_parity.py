@@ -102,3 +102,31 @@ def test_plan_device_pointers_and_stream(gpu, oracle):
         assert_same(d_out.cpu().numpy(), oracle_run(oracle, case), case)
         p2.close()
     plan.close()
+
+
+@pytest.mark.parametrize("kw", [dict(C=1, D=1, S=1, bits=8), dict(C=2, D=1, S=3, bits=4),
+                                dict(C=3, D=2, S=9, bits=1), dict(C=5, D=3, S=2, bits=16),
+                                dict(C=1, D=4, S=5, bits=32)])
+def test_degenerate_shapes_match_oracle(gpu, oracle, kw):
+    """One channel, one DM, a single sample: the tile machinery at its
+    smallest still equals the oracle."""
+    case = single_case(padding=0, zap=0.0, seed=31, **kw)
+    assert_same(engine_run(case), oracle_run(oracle, case), case)
+
+
+def test_zero_dms_is_empty_work(gpu):
+    """No DM trials: nothing to compute (the reference's loops run zero
+    times); the call succeeds and the plan path launches nothing."""
+    case = single_case(C=8, D=0, S=64, bits=8, padding=0, zap=0.0, seed=1)
+    assert case.out_elems == 0
+    out = np.zeros(0, np.float32)
+    dd.dedispersion(case.obs, case.zapped, case.mapping, case.inp, out, case.shifts, 0, 8)
+    p = dd.Plan(case.obs, dd.DD_SINGLE_STEP, 8, 0)
+    p.setShifts(case.shifts)
+    p.setZappedChannels(case.zapped)
+    p.setBeamMapping(case.mapping)
+    torch = pytest.importorskip("torch")
+    d_in = torch.from_numpy(case.inp).cuda()
+    p.run(d_in, 0)
+    p.check()
+    p.close()
