@@ -473,8 +473,10 @@ def _stream(s) -> int:
 
 
 class Batch:
-    """Many single-step problems (1/2/4/8-bit) in one persistent launch,
-    recorded as a CUDA graph at commit().  Device buffers are bound by add()."""
+    """Many single-step problems (1/2/4/8-bit) in one CUDA graph recorded at
+    commit(): the problems' own kernels on concurrent branches, or one
+    persistent direct-tile kernel where a problem does not fit the
+    shared-partial-sum tile.  Device buffers are bound by add()."""
 
     def __init__(self, device: int = 0):
         self._h = C.c_void_p()

@@ -291,9 +291,6 @@ struct dd_plan {
   // Created without a configuration: a shape that the default shared kernel
   // cannot take runs on the default direct kernel instead.
   bool auto_kernel = false;
-  // Shared memory per block kept free for a caller's kernel (the batch
-  // kernel's own static shared memory).
-  uint32_t smem_reserve = 0;
   // Tables changed since the last build: setters only record their table;
   // the first use (run, timing, queries) builds once.
   bool dirty = false;
@@ -452,7 +449,7 @@ dd_status rebuild(dd_plan *p) {
       return fail(DD_ERR_UNSUPPORTED, "kernel %s computes single-step 1/2/4/8-bit input only",
                   k.name);
     // One CTA per SM: the whole opt-in shared memory of a block.
-    const size_t budget = (size_t)dev_max - p->smem_reserve;
+    const size_t budget = (size_t)dev_max;
     (void)sm_max;
     const std::string why = dd::build_shared_tables(k, p->delay_shift, d.first_dm, d.dm_step,
                                                     d.nr_dms, p->bits, budget, &p->shared);
@@ -636,9 +633,6 @@ cudaError_t launch_row_stats(const ProblemDesc &P, unsigned long long *accum, ui
                              cudaStream_t stream);
 // Lets other translation units of the library report through dd_last_error.
 void set_last_error(const char *message) { g_error = message; }
-
-// Keep `bytes` of a block's shared memory free (before the tables are built).
-void plan_set_smem_reserve(dd_plan *p, uint32_t bytes) { p->smem_reserve = bytes; }
 
 // Makes `p` a stage of a subband pipeline with the packed intermediate: step
 // one writes pairs of coarse DMs; step two reads them with pair tile `k`,
