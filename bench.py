@@ -205,6 +205,7 @@ def bench_detect(torch, plan, d_in, d_out, stream, D, S, steps):
     import dedispersion_gb300 as dd
     d_acc = torch.empty((D, 3), dtype=torch.int64, device=d_out.device)
     n = max(3, min(steps, 20))
+    plan.setOverlap(False)  # both sides launched one after another
     for i in range(3):
         plan.run_stats(d_in[i % len(d_in)], d_out, d_acc, stream)
     e0 = torch.cuda.Event(enable_timing=True)
@@ -219,6 +220,7 @@ def bench_detect(torch, plan, d_in, d_out, stream, D, S, steps):
         plan.run_stats(d_in[i % len(d_in)], d_out, d_acc, stream)
     e2.record(stream)
     plan.check(stream)
+    plan.setOverlap(True)
     plain_ms, stats_ms = e0.elapsed_time(e1) / n, e1.elapsed_time(e2) / n
     st = dd.dm_stats(d_acc.cpu().numpy().view(np.uint64), S)
     best = int(np.argmax(st["snr"]))
@@ -526,6 +528,9 @@ def main():
     plan.setShifts(shifts)
     plan.setZappedChannels(zapped)
     plan.setBeamMapping(mapping)
+    # Consecutive steps are independent batches: each launch may start on the
+    # SMs the previous launch's last wave leaves idle (dd_plan_set_overlap).
+    plan.setOverlap(True)
     nbuf = 4
     d_in = [torch.from_numpy(inp).to(f"cuda:{local}") for _ in range(nbuf)]
     d_out = torch.empty(lay.output_bytes // 4, dtype=torch.float32, device=f"cuda:{local}")
@@ -555,6 +560,18 @@ def main():
     t_dev = max_over_ranks(ms / 1e3, pg, f"cuda:{local}")
     value = job_value(world, args.steps, D, S, t_dev)
     per_launch_s = t_dev / args.steps
+    # The same steps launched one after another (no overlap), for comparison.
+    plan.setOverlap(False)
+    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    e2.record(stream)
+    for i in range(args.steps):
+        plan.run(d_in[i % nbuf], d_out, stream)
+    e3.record(stream)
+    barrier()
+    plan.check(stream)
+    plan.setOverlap(True)
+    t_serial = max_over_ranks(e2.elapsed_time(e3) / 1e3, pg, f"cuda:{local}")
     if args.kernel_only:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -641,6 +658,10 @@ def main():
                                    f"channels), {cpu_dt:.2f} s wall on {cpu_threads} threads"},
         "clocks": clocks,
         "gpu_launches": args.steps * plan.launches(),
+        "serial_launches": {"ms_per_step": t_serial / args.steps * 1e3,
+                            "value": job_value(world, args.steps, D, S, t_serial),
+                            "what": "the same steps with dd_plan_set_overlap off: each launch "
+                                    "starts after the previous one completes"},
         "detect": detect,
         "ingest": ingest_line,
         "subband": subband,

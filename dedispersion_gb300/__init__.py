@@ -585,6 +585,11 @@ class Plan:
                                       C.c_void_p(_devptr(d_accum)),
                                       C.c_void_p(_stream(stream))))
 
+    def setOverlap(self, enable: bool = True) -> None:
+        """Launch runs as programmatic dependents of the stream's previous
+        kernel (dd_plan_set_overlap): only for consecutive independent runs."""
+        check(lib().dd_plan_set_overlap(self._h, 1 if enable else 0))
+
     def adds(self) -> int:
         """Integer adds one run performs (tile padding included)."""
         n = C.c_uint64(0)

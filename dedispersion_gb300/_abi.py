@@ -135,6 +135,7 @@ SIGNATURES = {
     "dd_plan_launches": (C.c_int, [_P, _U32P]),
     "dd_plan_get_conf": (C.c_int, [_P, _CONF]),
     "dd_plan_adds": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    "dd_plan_set_overlap": (C.c_int, [_P, C.c_int]),
     "dd_filterbank_info_read": (C.c_int, [C.c_char_p, _P]),
     "dd_filterbank_read": (C.c_int, [C.c_char_p, _P, C.c_uint64, C.c_uint64, _P]),
     "dd_filterbank_observation": (C.c_int, [_P, _P]),

@@ -299,6 +299,7 @@ struct dd_plan {
   bool packed = false;
   uint32_t flush_rows = 0;  // step two: rows per 16-bit lane flush
   uint32_t max_delay = 0;   // largest row delay of the built tables
+  bool overlap = false;     // dd_plan_set_overlap
 };
 
 namespace {
@@ -1032,8 +1033,32 @@ dd_status dd_plan_run(dd_plan *p, const void *d_input, float *d_output, void *st
   if (tiles == 0) return DD_OK;
   DeviceGuard g(p->device);
   if (!g.ok) return fail(DD_ERR_CUDA, "cannot select device %d", p->device);
+  if (p->overlap && p->kinfo->family == dd::kFamilyShared8) {
+    // A programmatic dependent of the stream's previous kernel: its tiles
+    // start on SMs the previous launch's last wave leaves idle.
+    P.overlap = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)tiles);
+    cfg.blockDim = dim3((unsigned)p->kinfo->threads);
+    cfg.dynamicSmemBytes = p->smem;
+    cfg.stream = static_cast<cudaStream_t>(stream);
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    void *args[] = {&P};
+    DD_CUDA(cudaLaunchKernelExC(&cfg, p->kinfo->func, args), "launch dedispersion kernel");
+    return DD_OK;
+  }
   p->kinfo->launch(P, (unsigned)tiles, p->smem, static_cast<cudaStream_t>(stream));
   DD_CUDA(cudaGetLastError(), "launch dedispersion kernel");
+  return DD_OK;
+}
+
+dd_status dd_plan_set_overlap(dd_plan *p, int enable) {
+  if (!p) return fail(DD_ERR_INVALID_ARGUMENT, "plan is NULL");
+  p->overlap = enable != 0;
   return DD_OK;
 }
 

@@ -119,6 +119,10 @@ struct ProblemDesc {
   // tile), the time tiles [ttile_base, ttile_base + ttile_count).
   uint32_t tile_base;
   uint32_t ttile_base, ttile_count;
+  // 1: launched as a programmatic dependent of the stream's previous kernel
+  // (dd_plan_set_overlap): the kernel lets the next launch start early and
+  // waits for the previous one before its first global write.
+  uint32_t overlap;
   uint32_t packed;
   uint32_t pair_groups;   // pairs of coarse DMs (groups per synthesized beam)
   uint32_t pair_d1;       // coarse DMs

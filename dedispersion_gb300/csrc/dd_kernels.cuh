@@ -48,6 +48,7 @@ template <int NW, int ND, int TY>
 __global__ void __launch_bounds__(32 * TY, (TY >= 16 ? 1 : 2))
     shared8_kernel(const ProblemDesc P) {
   extern __shared__ __align__(128) uint8_t smem[];
+  if (P.overlap) allow_dependents();
   const SharedLayout L = make_shared_layout(P.cw, P.psw, P.slots, P.table_bytes, P.bits);
   if (threadIdx.x == 0) {
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem);

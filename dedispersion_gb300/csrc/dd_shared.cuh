@@ -373,6 +373,9 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
   }
   sc += nst;
   flush();
+  // An overlapped launch writes only after the previous grid on the stream
+  // completed (it may still be writing the same output).
+  if (P.overlap) wait_prerequisites();
 
 #pragma unroll
   for (int j = 0; j < ND; ++j) {

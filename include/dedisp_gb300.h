@@ -321,6 +321,14 @@ dd_status dd_plan_get_conf(const dd_plan *plan, dd_conf *conf);
  * shared-partial-sum kernels (configurations with items_d2 = 8), which reach
  * the same sums with fewer adds.  No reference counterpart. */
 dd_status dd_plan_adds(const dd_plan *plan, uint64_t *adds);
+/* enable = 1: each dd_plan_run of this plan is launched as a programmatic
+ * dependent of the previous kernel on its stream, so that its tiles start on
+ * SMs the previous launch's last wave leaves idle; the kernel waits for the
+ * previous launch to complete before it writes anything.  Only for runs whose
+ * input is not written by the kernel launched just before them on the stream
+ * (consecutive independent batches).  Applies to the shared-partial-sum
+ * kernel; other kernels launch as usual.  Off by default. */
+dd_status dd_plan_set_overlap(dd_plan *plan, int enable);
 dd_status dd_plan_destroy(dd_plan *plan);
 
 /* ---- detection statistics of the output, computed in the same pass ------ */
