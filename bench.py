@@ -271,6 +271,61 @@ def bench_ingest(torch, inp, lay, obs, stream):
                     "descending-frequency file order reversed on the way"}
 
 
+def bench_float(torch, device: int, steps: int, peak_adds: float):
+    """Config 2 with float32 input (N(128, 20), same channels, DMs, zapping):
+    throughput of the float path (summed in the reference's channel order),
+    and its largest relative error against an FP64 sum of four DM rows
+    computed here with numpy."""
+    import dedispersion_gb300 as dd
+    from dedispersion_gb300 import synthetic as syn
+    obs = syn.large_observation(PADDING)
+    shifts = dd.getShifts(obs, PADDING)
+    zapped = syn.zapped_mask(1536, 0.05, 7, PADDING)
+    mapping = syn.identity_mapping(obs, PADDING)
+    lay = dd.layout(obs, dd.DD_SINGLE_STEP, 32, PADDING)
+    C, S, D = 1536, obs.getNrSamplesPerBatch(), obs.getNrDMs()
+    row = lay.input_row_bytes // 4
+    n = obs.getNrSamplesPerDispersedBatch()
+    g = torch.Generator(device=f"cuda:{device}")
+    g.manual_seed(5)
+    d_in = torch.zeros((C, row), dtype=torch.float32, device=f"cuda:{device}")
+    d_in[:, :n] = torch.randn((C, n), generator=g, device=f"cuda:{device}") * 20.0 + 128.0
+    d_out = torch.empty(lay.output_bytes // 4, dtype=torch.float32, device=f"cuda:{device}")
+    p = dd.Plan(obs, dd.DD_SINGLE_STEP, 32, PADDING, device=device)
+    p.setShifts(shifts)
+    p.setZappedChannels(zapped)
+    p.setBeamMapping(mapping)
+    stream = torch.cuda.current_stream()
+    for _ in range(2):
+        p.run(d_in, d_out, stream)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        p.run(d_in, d_out, stream)
+    e1.record(stream)
+    p.check(stream)
+    t = e0.elapsed_time(e1) / 1e3 / steps
+    # FP64 reference of DM rows 0, 700, 1400, 2047 (float32 delay arithmetic)
+    host = d_in.cpu().numpy().astype(np.float64)
+    out = d_out.cpu().numpy().reshape(D, -1)[:, :S]
+    live = np.flatnonzero(zapped[:C] == 0)
+    err = 0.0
+    for d in (0, 700, 1400, D - 1):
+        dm = np.float32(obs.getFirstDM()) + np.float32(d) * np.float32(obs.getDMStep())
+        delay = (np.float32(dm) * shifts[live].astype(np.float32)).astype(np.uint32)
+        ref = np.zeros(S, np.float64)
+        for c, dl in zip(live, delay):
+            ref += host[c, dl:dl + S]
+        err = max(err, float(np.max(np.abs(out[d] - ref) / np.abs(ref))))
+    p.close()
+    adds = D * S * len(live)
+    return {"value": D * S / t, "unit": UNIT, "ms_per_step": t * 1e3, "dtype": "f32",
+            "adds_frac": adds / t / peak_adds, "max_rel_err_vs_fp64": err,
+            "tolerance": 1e-5, "kernel": "scalar float tile",
+            "workload": "1536 ch x 2048 DM x 24576 samples, float32 N(128, 20), 5% zapped"}
+
+
 def bench_subband(torch, device: int, steps: int, hbm_peak: float, peak_adds: float):
     """Config 2 in subband mode (1536 ch in 32 subbands, 64 coarse DMs at 6.4
     x 32 fine DMs at 0.2, 24576 samples, uint8 N(128, 20), 5 % zapped): the
@@ -606,6 +661,7 @@ def main():
     detect = bench_detect(torch, plan, d_in, d_out, stream, D, S, args.steps)
     ingest_line = bench_ingest(torch, inp, lay, obs, stream)
     subband = bench_subband(torch, local, max(10, min(args.steps, 50)), hbm_peak, peak_adds)
+    float32 = bench_float(torch, local, max(3, min(args.steps, 10)), peak_adds)
     batched = bench_batched(torch, local, peak_adds=peak_adds) if not args.no_batched else None
     served = bench_served(local) if not args.no_served else None
 
@@ -665,6 +721,7 @@ def main():
         "detect": detect,
         "ingest": ingest_line,
         "subband": subband,
+        "float32": float32,
         "batched": batched,
         "served": served,
     }
