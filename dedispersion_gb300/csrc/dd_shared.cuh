@@ -56,9 +56,10 @@ constexpr uint32_t kItemsMax = 32;                      // phase-A items per sta
 //   programs (u32, 16-byte aligned): n | ng << 16, nA | nB << 16, dst of
 //   chain A's first vector, dst of chain B's (~0: no chain B), 8 copy-area
 //   byte offsets of A's first vector's rows, 8 of B's, then nA and nB
-//   micro-ops of 4 u32: (old byte offset, new byte offset, dst, 0); dst is
-//   where the series stands after the micro-op (the dummy series when the
-//   vector is not complete yet); nA == nB whenever chain B exists
+//   micro-ops of 4 u32: (old byte offset, new byte offset, dst, real); dst is
+//   where the series stands after the micro-op, real = 1 when the vector is
+//   complete (else dst is the dummy series and nothing is stored); nA == nB
+//   whenever chain B exists
 constexpr uint32_t kTabItems = 8 + 4 * kSubMax;
 constexpr uint32_t kTabSeries = kTabItems + kItemsMax;
 static_assert(kTabSeries % 8 == 0, "series offsets 16-byte aligned");
@@ -307,7 +308,6 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
       // dummy series).
       const uint32_t keep = (tx < 31 && g < ng) ? 1u : 0u;
       const uint32_t pg = part_s + 8u * g;
-      const uint32_t dummy = 4u * L.dummy_word;
       // lo = (P[4g], P[4g+1]), hi = (P[4g+2], P[4g+3]) as 16-bit lanes.
       uint32_t loA = 0, hiA = 0, loB = 0, hiB = 0;
       auto rows = [&](const uint32_t *offs, uint32_t &lo, uint32_t &hi) {
@@ -321,9 +321,11 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
           hi = mad_lo(__byte_perm(w, 0, 0x4342), one, hi);
         }
       };
-      auto store = [&](uint32_t dst, uint32_t lo, uint32_t hi) {
+      // `real` = 0 for micro-ops whose vector is not complete yet (their dst
+      // is the dummy series; the host sets the flag in the micro-op).
+      auto store = [&](uint32_t dst, uint32_t real, uint32_t lo, uint32_t hi) {
         const uint32_t nlo = __shfl_down_sync(0xffffffffu, lo, 1);
-        const uint32_t on = keep & (dst != dummy ? 1u : 0u);
+        const uint32_t on = keep & real;
         sts_v2_if(on, pg + dst, lo, hi);
         sts_v2_if(on, pg + dst + 4u * psw, __byte_perm(lo, hi, 0x5432),
                   __byte_perm(hi, nlo, 0x5432));
@@ -336,8 +338,8 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
       };
       rows(prog + 4, loA, hiA);
       if (hasB) rows(prog + 12, loB, hiB);
-      store(hdr.z, loA, hiA);
-      if (hasB) store(hdr.w, loB, hiB);
+      store(hdr.z, 1u, loA, hiA);
+      if (hasB) store(hdr.w, 1u, loB, hiB);
       // Chain B exists whenever there are micro-ops; the host pads the two
       // halves to the same length with no-op micro-ops.
       const uint4 *ua = reinterpret_cast<const uint4 *>(prog + 20);
@@ -346,8 +348,8 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
         const uint4 a = ua[i], b = ub[i];
         step(a, loA, hiA);
         step(b, loB, hiB);
-        store(a.z, loA, hiA);
-        store(b.z, loB, hiB);
+        store(a.z, a.w, loA, hiA);
+        store(b.z, b.w, loB, hiB);
       }
     }
     __syncthreads();

@@ -328,7 +328,7 @@ std::string build_shared_tables(const KernelInfo &k, const std::vector<float> &r
                 u.push_back(off(e, s.vec[v - 1][e]));
                 u.push_back(off(e, s.vec[v][e]));
                 u.push_back(--left == 0 ? dst_of(v) : dummy_bytes);
-                u.push_back(0);
+                u.push_back(left == 0 ? 1u : 0u);  // 1: the store is real
               }
           }
         };

@@ -205,6 +205,8 @@ int main(int argc, char **argv) {
               for (uint32_t i = 0; i < nu; i++) {
                 const uint32_t o = T32(u0 + 8 * i), nw = T32(u0 + 8 * i + 2);
                 const uint32_t dst = T32(u0 + 8 * i + 4);
+                if (T32(u0 + 8 * i + 6) != (dst / 4 != dummy0 ? 1u : 0u))
+                  return fail("store flag", s, q, i);
                 for (uint32_t lane = 0; lane < 32; lane++) {
                   const uint32_t g = std::min(c * 31 + lane, ng - 1);
                   uint32_t wo, wn;
