@@ -370,6 +370,12 @@ def bench_subband(torch, device: int, steps: int, hbm_peak: float, peak_adds: fl
 
     t_pipe = timed(lambda i: pipe.run(d_in[i % nbuf], out, stream))
     pipe.check(stream)
+    # consecutive independent batches: step one may start during the previous
+    # batch's step two (dd_subband_set_overlap)
+    pipe.setOverlap(True)
+    t_pipe_ov = timed(lambda i: pipe.run(d_in[i % nbuf], out, stream))
+    pipe.check(stream)
+    pipe.setOverlap(False)
     t_float = timed(lambda i: (one.run(d_in[i % nbuf], inter, stream),
                                two.run(inter, ref, stream)))
     two.check(stream)
@@ -387,13 +393,15 @@ def bench_subband(torch, device: int, steps: int, hbm_peak: float, peak_adds: fl
     hbm_bytes = inp.nbytes + 2 * info["intermediate_bytes"] + D1 * D2 * S * 4
     for x in (pipe, one, two):
         x.close()
-    return {"value": units / t_pipe, "unit": UNIT, "ms_per_batch": t_pipe * 1e3,
+    return {"value": units / t_pipe_ov, "unit": UNIT, "ms_per_batch": t_pipe_ov * 1e3,
+            "serial_value": units / t_pipe, "serial_ms_per_batch": t_pipe * 1e3,
             "float_steps_value": units / t_float, "float_steps_ms": t_float * 1e3,
             "speedup_vs_float_steps": t_float / t_pipe, "bit_exact_vs_float_steps": exact,
+            "note_speedup": "serial pipeline against the serial float steps",
             "packed": info["packed"], "intermediate_bytes": info["intermediate_bytes"],
-            "adds_per_batch": adds, "adds_frac": adds / t_pipe / peak_adds,
+            "adds_per_batch": adds, "adds_frac": adds / t_pipe_ov / peak_adds,
             "hbm_bytes_upper": hbm_bytes,
-            "hbm_frac_upper": hbm_bytes / t_pipe / 1e9 / hbm_peak,
+            "hbm_frac_upper": hbm_bytes / t_pipe_ov / 1e9 / hbm_peak,
             "gpu_launches_per_batch": 2,
             "workload": "1536 ch in 32 subbands (5% zapped), 64 coarse DMs at 6.4 x 32 fine "
                         "DMs at 0.2 = 2048 DMs, 24576 samples, uint8 N(128, 20)",

@@ -364,6 +364,11 @@ class SubbandPipeline:
                                           _ptr(z, C.c_uint32), z.size, _ptr(m, C.c_uint32),
                                           m.size))
 
+    def setOverlap(self, enable: bool = True) -> None:
+        """Let step one of each run start while the previous run's step two
+        finishes (dd_subband_set_overlap): consecutive independent runs only."""
+        check(lib().dd_subband_set_overlap(self._h, 1 if enable else 0))
+
     def setPairKernel(self, index: int) -> None:
         check(lib().dd_subband_set_pair_kernel(self._h, int(index)))
 

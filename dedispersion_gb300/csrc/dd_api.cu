@@ -1033,7 +1033,9 @@ dd_status dd_plan_run(dd_plan *p, const void *d_input, float *d_output, void *st
   if (tiles == 0) return DD_OK;
   DeviceGuard g(p->device);
   if (!g.ok) return fail(DD_ERR_CUDA, "cannot select device %d", p->device);
-  if (p->overlap && p->kinfo->family == dd::kFamilyShared8) {
+  // The shared, swar8 and pair tiles take part (the scalar tile launches as
+  // usual).
+  if (p->overlap && p->kinfo->family != dd::kFamilyScalar) {
     // A programmatic dependent of the stream's previous kernel: its tiles
     // start on SMs the previous launch's last wave leaves idle.
     P.overlap = 1;

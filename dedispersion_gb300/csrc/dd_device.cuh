@@ -549,6 +549,8 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
   }
   sc += nst;
   flush();
+  // An overlapped launch writes only after the previous grid completed.
+  if (P.overlap) wait_prerequisites();
 
   if (P.packed) {
     // Pairs (2p, 2p + 1) of the thread's DMs (d0 and NDT even): exact sums
@@ -836,6 +838,7 @@ __device__ __forceinline__ bool pair_tile(const ProblemDesc &P, uint32_t g,
   }
   sc += nst;
   widen();
+  if (P.overlap) wait_prerequisites();
 
   const bool hi_ok = (g % P.pair_groups) * 2u + 1u < P.pair_d1;
 #pragma unroll

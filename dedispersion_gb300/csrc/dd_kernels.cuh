@@ -15,6 +15,7 @@ template <int NW, int NDT, int TY, int CH, int VAR>
 __global__ void __launch_bounds__(32 * TY, (TY >= 16 ? 1 : (TY >= 8 ? 2 : 4)))
     swar8_kernel(const ProblemDesc P) {
   extern __shared__ __align__(128) uint8_t smem[];
+  if (P.overlap) allow_dependents();
   const SmemLayout L = make_layout(kFamilySwar8, P.win_samples, P.bits, CH, TY * NDT);
   init_barriers(smem, L, CH);
   uint32_t g, dtile, ttile, sc = 0;
@@ -37,6 +38,7 @@ template <int NS, int NDT, int TY, int CH, int MINB>
 __global__ void __launch_bounds__(32 * TY, MINB)
     pair_kernel(const ProblemDesc P) {
   extern __shared__ __align__(128) uint8_t smem[];
+  if (P.overlap) allow_dependents();
   const SmemLayout L = make_layout(kFamilyPair16, P.win_samples, 32, CH, TY * NDT);
   init_barriers(smem, L, CH);
   uint32_t g, dtile, ttile, sc = 0;

@@ -107,6 +107,7 @@ struct dd_subband {
   bool packed = false;
   bool ready = false;
   int pair_kernel = 0;  // index into dd::pair_kernels
+  bool overlap = false;  // step one as a programmatic dependent
   void *inter = nullptr;  // step-one output (packed or float)
   size_t inter_bytes = 0;
   std::vector<float> shifts, shifts2;
@@ -130,6 +131,7 @@ dd_status make_plans(dd_subband *s) {
   if (!st) st = dd_plan_set_zapped(s->one, s->zapped.data(), s->zapped.size());
   if (!st) st = dd_plan_set_shifts(s->two, s->shifts2.data(), s->shifts2.size());
   if (!st) st = dd_plan_set_beam_mapping(s->two, s->mapping.data(), s->mapping.size());
+  if (!st) st = dd_plan_set_overlap(s->one, s->overlap ? 1 : 0);
   return st;
 }
 
@@ -258,6 +260,12 @@ dd_status dd_subband_set_pair_kernel(dd_subband *s, int index) {
     return fail(DD_ERR_INVALID_ARGUMENT, "pair kernel %d out of range (0..%d)", index, n - 1);
   s->pair_kernel = index;
   return s->shifts.empty() ? DD_OK : build(s);
+}
+
+dd_status dd_subband_set_overlap(dd_subband *s, int enable) {
+  if (!s) return fail(DD_ERR_INVALID_ARGUMENT, "pipeline is NULL");
+  s->overlap = enable != 0;
+  return s->one ? dd_plan_set_overlap(s->one, enable) : DD_OK;
 }
 
 int dd_subband_pair_kernel_count(void) {

@@ -238,6 +238,12 @@ dd_status dd_subband_check(dd_subband *pipeline, void *stream);
 /* Whether the intermediate is packed, and its device bytes. */
 dd_status dd_subband_info(const dd_subband *pipeline, int *packed,
                           uint64_t *intermediate_bytes);
+/* enable = 1: step one of each run is launched as a programmatic dependent of
+ * the kernel before it on the stream (dd_plan_set_overlap), so that it starts
+ * while the previous run's step two finishes; it writes the intermediate only
+ * after that step two completed.  Only for runs whose input the kernel before
+ * them does not write.  Off by default. */
+dd_status dd_subband_set_overlap(dd_subband *pipeline, int enable);
 /* Tile configuration of the packed step two (0 .. count - 1; 0 default). */
 dd_status dd_subband_set_pair_kernel(dd_subband *pipeline, int index);
 int dd_subband_pair_kernel_count(void);
@@ -326,8 +332,9 @@ dd_status dd_plan_adds(const dd_plan *plan, uint64_t *adds);
  * SMs the previous launch's last wave leaves idle; the kernel waits for the
  * previous launch to complete before it writes anything.  Only for runs whose
  * input is not written by the kernel launched just before them on the stream
- * (consecutive independent batches).  Applies to the shared-partial-sum
- * kernel; other kernels launch as usual.  Off by default. */
+ * (consecutive independent batches).  Applies to the shared-partial-sum and
+ * 1/2/4/8-bit direct kernels; the 16-bit and float kernels launch as usual.
+ * Off by default. */
 dd_status dd_plan_set_overlap(dd_plan *plan, int enable);
 dd_status dd_plan_destroy(dd_plan *plan);
 

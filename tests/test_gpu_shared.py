@@ -158,17 +158,23 @@ def test_full_workload_equals_direct_kernel(gpu):
     assert min(adds[1:]) < adds[0] / 2
 
 
-def test_overlapped_runs_equal_serial_runs(gpu):
+@pytest.mark.parametrize("family", ["shared", "direct"])
+def test_overlapped_runs_equal_serial_runs(gpu, family):
     """dd_plan_set_overlap: consecutive runs launched as programmatic
-    dependents (3.4 waves each) give the serial runs' outputs, also when two
-    consecutive runs write the same output buffer."""
+    dependents (several waves each) give the serial runs' outputs, also when
+    two consecutive runs write the same output buffer; shared and direct
+    tiles."""
     torch = pytest.importorskip("torch")
+    kidx = None
+    if family == "direct":
+        kidx = next(k.index for k in dd.kernels()
+                    if k.elem_bits == 8 and k.conf.getNrItemsD2() != 8)
     a = single_case(C=512, D=512, S=16384, bits=8, padding=128, zap=0.05, seed=41, dist="uniform")
     b = single_case(C=512, D=512, S=16384, bits=8, padding=128, zap=0.05, seed=42, dist="uniform")
     assert np.array_equal(a.shifts, b.shifts)
 
     def plan(overlap):
-        p = dd.Plan(a.obs, dd.DD_SINGLE_STEP, 8, 128)
+        p = dd.Plan(a.obs, dd.DD_SINGLE_STEP, 8, 128, kernel=kidx)
         p.setShifts(a.shifts)
         p.setZappedChannels(a.zapped)
         p.setBeamMapping(a.mapping)

@@ -155,3 +155,35 @@ def test_full_shape_equals_float_steps(gpu):
     assert torch.equal(got, want)
     for x in (p, one, two):
         x.close()
+
+
+def test_overlapped_pipeline_runs_equal_serial_runs(gpu):
+    """dd_subband_set_overlap: step one of each run starts while the
+    previous run's step two finishes; outputs equal serial runs."""
+    torch = pytest.importorskip("torch")
+    obs, shifts, shifts2, zapped, inp_a, mapping = _case(bits=8, padding=64, seed=21, D1=16,
+                                                           D2=32, S=4096, C=512, SB=16)
+    inp_b = syn.make_input(obs, 8, 64, 22, mode=dd.DD_STEP_ONE)
+
+    def pipe(overlap):
+        p = dd.SubbandPipeline(obs, 8, 64)
+        p.setTables(shifts, shifts2, zapped, mapping)
+        p.setOverlap(overlap)
+        return p
+
+    d_a, d_b = torch.from_numpy(inp_a).cuda(), torch.from_numpy(inp_b).cuda()
+    serial, ov = pipe(False), pipe(True)
+    new = lambda: torch.zeros(serial.layout_out.output_bytes // 4, dtype=torch.float32,
+                              device="cuda")
+    want_a, want_b = new(), new()
+    serial.run(d_a, want_a)
+    serial.run(d_b, want_b)
+    serial.check()
+    out_a, out_b = new(), new()
+    for _ in range(4):
+        ov.run(d_a, out_a)
+        ov.run(d_b, out_b)
+    ov.check()
+    assert torch.equal(out_a, want_a) and torch.equal(out_b, want_b)
+    serial.close()
+    ov.close()
