@@ -121,6 +121,51 @@ bool dada_keys(std::ifstream &in, uint64_t bytes, std::map<std::string, std::str
   return true;
 }
 
+// Word-wide transpose for 4-byte aligned blocks (nchans, the row pitch and
+// the sample offset multiples of 4): 64 samples x 64 channels per CTA of 256
+// threads.  Loads and stores are 32-bit and coalesced (16 words per time row
+// or channel row); each thread transposes a 4 x 4 byte block (4 samples x 4
+// channels) in registers with byte permutes.
+__global__ void __launch_bounds__(256) transpose8x4_kernel(
+    const uint32_t *__restrict__ src, uint32_t count, uint32_t nchans, int reverse,
+    uint8_t *__restrict__ dst, uint64_t row_bytes, uint64_t offset) {
+  __shared__ uint32_t tile[64][17];  // [sample][channel word], padded
+  const uint32_t t0 = blockIdx.x * 64, c0 = blockIdx.y * 64;
+  const uint32_t tid = threadIdx.x, cwords = nchans / 4;
+#pragma unroll
+  for (uint32_t j = 0; j < 4; j++) {
+    const uint32_t r = tid / 16 + 16 * j, col = tid % 16;
+    const uint32_t t = t0 + r, cw = c0 / 4 + col;
+    tile[r][col] = (t < count && cw < cwords) ? src[(uint64_t)t * cwords + cw] : 0u;
+  }
+  __syncthreads();
+  // One 4 x 4 byte block per thread: sample word sw (samples 4 sw .. +3) of
+  // channel word cword (channels 4 cword .. +3); 16 x 16 blocks per tile.
+  const uint32_t sw = tid % 16, cword = tid / 16;
+  const uint32_t w0 = tile[4 * sw][cword], w1 = tile[4 * sw + 1][cword];
+  const uint32_t w2 = tile[4 * sw + 2][cword], w3 = tile[4 * sw + 3][cword];
+  // w_k = channels 4 cword .. +3 of sample 4 sw + k; out[m] = channel m's
+  // four samples
+  const uint32_t a = __byte_perm(w0, w1, 0x5140), b = __byte_perm(w0, w1, 0x7362);
+  const uint32_t c = __byte_perm(w2, w3, 0x5140), d = __byte_perm(w2, w3, 0x7362);
+  const uint32_t out[4] = {__byte_perm(a, c, 0x5410), __byte_perm(a, c, 0x7632),
+                           __byte_perm(b, d, 0x5410), __byte_perm(b, d, 0x7632)};
+  const uint32_t t = t0 + 4 * sw;
+  if (t >= count) return;
+#pragma unroll
+  for (uint32_t m = 0; m < 4; m++) {
+    const uint32_t ch = c0 + 4 * cword + m;
+    if (ch >= nchans) break;
+    const uint32_t row = reverse ? nchans - 1 - ch : ch;
+    uint8_t *p = dst + (uint64_t)row * row_bytes + offset + t;
+    if (t + 3 < count) {
+      *reinterpret_cast<uint32_t *>(p) = out[m];
+    } else {
+      for (uint32_t k = 0; t + k < count; k++) p[k] = (uint8_t)(out[m] >> (8 * k));
+    }
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -311,10 +356,20 @@ dd_status dd_transpose_time_major(const void *d_src, uint32_t count, uint32_t nc
                 (unsigned long long)(dst_sample_offset + count),
                 (unsigned long long)dst_row_bytes);
   if (count == 0 || nchans == 0) return DD_OK;
-  const dim3 grid((count + 31) / 32, (nchans + 31) / 32), block(32, 8);
-  transpose8_kernel<<<grid, block, 0, static_cast<cudaStream_t>(stream)>>>(
-      static_cast<const uint8_t *>(d_src), count, nchans, reverse,
-      static_cast<uint8_t *>(d_dst), dst_row_bytes, dst_sample_offset);
+  const bool words = nchans % 4 == 0 && dst_row_bytes % 4 == 0 && dst_sample_offset % 4 == 0 &&
+                     reinterpret_cast<uintptr_t>(d_src) % 4 == 0 &&
+                     reinterpret_cast<uintptr_t>(d_dst) % 4 == 0;
+  if (words) {
+    const dim3 grid((count + 63) / 64, (nchans + 63) / 64);
+    transpose8x4_kernel<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const uint32_t *>(d_src), count, nchans, reverse,
+        static_cast<uint8_t *>(d_dst), dst_row_bytes, dst_sample_offset);
+  } else {
+    const dim3 grid((count + 31) / 32, (nchans + 31) / 32), block(32, 8);
+    transpose8_kernel<<<grid, block, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const uint8_t *>(d_src), count, nchans, reverse,
+        static_cast<uint8_t *>(d_dst), dst_row_bytes, dst_sample_offset);
+  }
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(DD_ERR_CUDA, "launch transpose: %s", cudaGetErrorString(e));
   return DD_OK;

@@ -123,17 +123,21 @@ def test_dada_rejects_what_it_cannot_read(tmp_path):
 
 
 @pytest.mark.gpu
-def test_device_transpose(gpu, tmp_path):
+@pytest.mark.parametrize("nchans,samples,row_bytes,offset", [
+    (200, 1000, 1280, 100),   # 4-byte aligned: the word kernel
+    (200, 1003, 1280, 100),   # word kernel, ragged last sample word
+    (198, 1000, 1283, 101),   # unaligned: the byte kernel
+])
+def test_device_transpose(gpu, tmp_path, nchans, samples, row_bytes, offset):
     torch = pytest.importorskip("torch")
-    path, data = _file(tmp_path, samples=1000, nchans=200, seed=4)
+    path, data = _file(tmp_path, samples=samples, nchans=nchans, seed=4)
     fb = ingest.Filterbank(path)
-    row_bytes, offset = 1280, 100
-    d_rows = torch.zeros(200 * row_bytes, dtype=torch.uint8, device="cuda")
-    fb.to_rows(torch.from_numpy(fb.read(0, 1000).copy()).cuda(), d_rows, row_bytes, offset)
+    d_rows = torch.zeros(nchans * row_bytes, dtype=torch.uint8, device="cuda")
+    fb.to_rows(torch.from_numpy(fb.read(0, samples).copy()).cuda(), d_rows, row_bytes, offset)
     torch.cuda.synchronize()
-    rows = d_rows.cpu().numpy().reshape(200, row_bytes)
-    np.testing.assert_array_equal(rows[:, offset:offset + 1000], data.T[::-1])
-    assert not rows[:, :offset].any() and not rows[:, offset + 1000:].any()
+    rows = d_rows.cpu().numpy().reshape(nchans, row_bytes)
+    np.testing.assert_array_equal(rows[:, offset:offset + samples], data.T[::-1])
+    assert not rows[:, :offset].any() and not rows[:, offset + samples:].any()
 
 
 @pytest.mark.gpu
