@@ -482,7 +482,8 @@ def bench_batched(torch, device: int, reps: int = 3, count: int = 40, peak_adds:
                         "0.1-0.5, 2/4/8-bit uniform input, 5% zapped"}
 
 
-def bench_served(device: int, batches: int = 6, compression: float = 16.0):
+def bench_served(device: int, batches: int = 6, compression: float = 16.0,
+                 double_buffer: bool = True):
     """12 beams streaming 2.048 s batches (1536 ch, 25000 samples at 81.92 us,
     8-bit), DM ranges of 1024-4096 DMs at step 0.2, alternating single-step and
     subband (32 subbands) modes, admitted against a 150 GB budget.  Two runs:
@@ -494,7 +495,8 @@ def bench_served(device: int, batches: int = 6, compression: float = 16.0):
     for b in range(12):
         dms = int(rng.integers(8, 33)) * 128
         cfgs.append(serving.BeamConfig(name=f"beam{b}", dms=dms, subband=(b % 2 == 1),
-                                       seed=100 + b, padding=PADDING))
+                                       seed=100 + b, padding=PADDING,
+                                       double_buffer=double_buffer))
     server = serving.Server(budget_bytes=150 * 10**9, device=device)
     for c in cfgs:
         server.admit(c)
@@ -523,6 +525,7 @@ def bench_served(device: int, batches: int = 6, compression: float = 16.0):
            "offered_load_throughput": lat["throughput_dm_samples_per_s"],
            "beams": len(cfgs), "subband_beams": sum(c.subband for c in cfgs),
            "admitted_device_bytes": server.used, "budget_bytes": server.budget,
+           "double_buffered": double_buffer,
            "workload": "12 beams x 25000-sample 8-bit batches, 1536 ch, 1024-4096 DMs at 0.2, "
                        "single-step and 32-subband streams, tail carried on the device; value = "
                        "all batches queued at once, latency = Poisson-jittered arrivals at 16x "

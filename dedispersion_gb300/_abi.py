@@ -166,6 +166,9 @@ SIGNATURES = {
                                  _U32P]),
     "dd_stream_push": (C.c_int, [_P, _P]),
     "dd_stream_set_time_major": (C.c_int, [_P, C.c_int]),
+    "dd_stream_set_double_buffer": (C.c_int, [_P, C.c_int]),
+    "dd_stream_buffer": (C.c_int, [_P, C.c_int, C.POINTER(_P), C.POINTER(_P)]),
+    "dd_stream_next_buffer": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "dd_stream_destroy": (C.c_int, [_P]),
     "dd_mlp_create": (C.c_int, [C.POINTER(_P), C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64,
                                 C.c_int]),

@@ -149,14 +149,17 @@ struct dd_stream {
   dd_plan *plan1 = nullptr, *plan2 = nullptr;
   uint8_t *d_ring = nullptr;
   float *d_mid = nullptr, *d_out = nullptr;
-  uint8_t *h_in = nullptr;
-  float *h_out = nullptr;
+  // Pinned staging input and output, one pair per buffer; push k uses pair
+  // k % nbuf (dd_stream_set_double_buffer: nbuf = 2).
+  uint8_t *h_in[2] = {nullptr, nullptr};
+  float *h_out[2] = {nullptr, nullptr};
+  int nbuf = 1, next = 0;
   uint64_t device_bytes = 0;
   uint64_t in_row_bytes = 0;  // staging row: S samples
   uint32_t out_rows = 0;
   cudaStream_t capture = nullptr;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph[2] = {nullptr, nullptr};
+  cudaGraphExec_t exec[2] = {nullptr, nullptr};
   // Time-major input (dd_stream_set_time_major): the staged block [S][C] is
   // copied to d_block and transposed into the ring.
   bool time_major = false;
@@ -167,16 +170,20 @@ struct dd_stream {
 namespace {
 
 void release(dd_stream *s) {
-  if (s->exec) cudaGraphExecDestroy(s->exec);
-  if (s->graph) cudaGraphDestroy(s->graph);
+  for (int b = 0; b < 2; b++) {
+    if (s->exec[b]) cudaGraphExecDestroy(s->exec[b]);
+    if (s->graph[b]) cudaGraphDestroy(s->graph[b]);
+  }
   if (s->capture) cudaStreamDestroy(s->capture);
   if (s->plan1) dd_plan_destroy(s->plan1);
   if (s->plan2) dd_plan_destroy(s->plan2);
   if (s->d_ring) cudaFree(s->d_ring);
   if (s->d_mid) cudaFree(s->d_mid);
   if (s->d_out) cudaFree(s->d_out);
-  if (s->h_in) cudaFreeHost(s->h_in);
-  if (s->h_out) cudaFreeHost(s->h_out);
+  for (int b = 0; b < 2; b++) {
+    if (s->h_in[b]) cudaFreeHost(s->h_in[b]);
+    if (s->h_out[b]) cudaFreeHost(s->h_out[b]);
+  }
   if (s->d_block) cudaFree(s->d_block);
 }
 
@@ -194,38 +201,42 @@ uint64_t total_bytes(const Geometry &g, int subband) {
   return b;
 }
 
-dd_status enqueue(dd_stream *s, cudaStream_t st);
+dd_status enqueue(dd_stream *s, cudaStream_t st, int buf);
 
-// (Re-)records the push as a graph.
+// (Re-)records the push as a graph, one per staging buffer.
 dd_status record(dd_stream *s) {
-  if (s->exec) cudaGraphExecDestroy(s->exec);
-  if (s->graph) cudaGraphDestroy(s->graph);
-  s->exec = nullptr;
-  s->graph = nullptr;
+  for (int b = 0; b < 2; b++) {
+    if (s->exec[b]) cudaGraphExecDestroy(s->exec[b]);
+    if (s->graph[b]) cudaGraphDestroy(s->graph[b]);
+    s->exec[b] = nullptr;
+    s->graph[b] = nullptr;
+  }
   if (!s->capture) DDS_CUDA(cudaStreamCreateWithFlags(&s->capture, cudaStreamNonBlocking), "create stream");
-  DDS_CUDA(cudaStreamBeginCapture(s->capture, cudaStreamCaptureModeThreadLocal), "begin capture");
-  dd_status st = enqueue(s, s->capture);
-  cudaError_t e = cudaStreamEndCapture(s->capture, &s->graph);
-  if (st) return st;
-  if (e == cudaSuccess) e = cudaGraphInstantiate(&s->exec, s->graph, 0);
-  if (e != cudaSuccess) return cuda_fail(e, "record stream graph");
+  for (int b = 0; b < s->nbuf; b++) {
+    DDS_CUDA(cudaStreamBeginCapture(s->capture, cudaStreamCaptureModeThreadLocal), "begin capture");
+    dd_status st = enqueue(s, s->capture, b);
+    cudaError_t e = cudaStreamEndCapture(s->capture, &s->graph[b]);
+    if (st) return st;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&s->exec[b], s->graph[b], 0);
+    if (e != cudaSuccess) return cuda_fail(e, "record stream graph");
+  }
   return DD_OK;
 }
 
-dd_status enqueue(dd_stream *s, cudaStream_t st) {
+dd_status enqueue(dd_stream *s, cudaStream_t st, int buf) {
   const Geometry &g = s->g;
   const uint32_t C = g.one.nr_channels, S = g.one.nr_samples_per_batch;
   const uint64_t tail_b = bytes_of(g.tail, s->bits), new_b = bytes_of(S, s->bits);
   // 1. new samples after the tail (channel rows, or a time-major block
   //    transposed into the rows on the device)
   if (s->time_major) {
-    DDS_CUDA(cudaMemcpyAsync(s->d_block, s->h_in, (size_t)S * C, cudaMemcpyHostToDevice, st),
+    DDS_CUDA(cudaMemcpyAsync(s->d_block, s->h_in[buf], (size_t)S * C, cudaMemcpyHostToDevice, st),
              "copy batch");
     dd_status r = dd_transpose_time_major(s->d_block, S, C, s->reverse, s->d_ring,
                                           g.ring.input_row_bytes, g.tail, st);
     if (r) return r;
   } else {
-    DDS_CUDA(cudaMemcpy2DAsync(s->d_ring + tail_b, g.ring.input_row_bytes, s->h_in,
+    DDS_CUDA(cudaMemcpy2DAsync(s->d_ring + tail_b, g.ring.input_row_bytes, s->h_in[buf],
                                s->in_row_bytes, new_b, C, cudaMemcpyHostToDevice, st),
              "copy batch to ring");
   }
@@ -234,7 +245,7 @@ dd_status enqueue(dd_stream *s, cudaStream_t st) {
   if (!r && s->subband) r = dd_plan_run(s->plan2, s->d_mid, s->d_out, st);
   if (r) return r;
   // 3. valid output samples to the pinned host rows
-  DDS_CUDA(cudaMemcpy2DAsync(s->h_out, (size_t)S * 4, s->d_out, g.out.output_row_elems * 4,
+  DDS_CUDA(cudaMemcpy2DAsync(s->h_out[buf], (size_t)S * 4, s->d_out, g.out.output_row_elems * 4,
                              (size_t)S * 4, s->out_rows, cudaMemcpyDeviceToHost, st),
            "copy output");
   // 4. carry the tail to the front (source and destination do not overlap: S >= tail)
@@ -317,13 +328,13 @@ dd_status dd_stream_create(dd_stream **out, const dd_observation *obs, int subba
   if (e == cudaSuccess) e = cudaMemset(s->d_ring, 0, g.ring.input_bytes);
   if (e == cudaSuccess) e = cudaMalloc(&s->d_out, g.out.output_bytes);
   if (e == cudaSuccess && s->subband) e = cudaMalloc(&s->d_mid, mid_bytes(g));
-  if (e == cudaSuccess) e = cudaHostAlloc(&s->h_in, s->in_row_bytes * C, cudaHostAllocDefault);
+  if (e == cudaSuccess) e = cudaHostAlloc(&s->h_in[0], s->in_row_bytes * C, cudaHostAllocDefault);
   if (e == cudaSuccess) e = cudaMemset(s->d_out, 0, g.out.output_bytes);
   if (e == cudaSuccess)
-    e = cudaHostAlloc(reinterpret_cast<void **>(&s->h_out), (size_t)S * 4 * s->out_rows,
+    e = cudaHostAlloc(reinterpret_cast<void **>(&s->h_out[0]), (size_t)S * 4 * s->out_rows,
                       cudaHostAllocDefault);
   if (e != cudaSuccess) return bail(cuda_fail(e, "allocate stream buffers"));
-  std::memset(s->h_in, 0, s->in_row_bytes * C);
+  std::memset(s->h_in[0], 0, s->in_row_bytes * C);
   s->device_bytes = total_bytes(g, s->subband);
   st = record(s);
   if (st) return bail(st);
@@ -345,8 +356,8 @@ dd_status dd_stream_set_time_major(dd_stream *s, int reverse) {
 
 dd_status dd_stream_buffers(dd_stream *s, void **h_input, float **h_output, float **d_output) {
   if (!s) return fail(DD_ERR_INVALID_ARGUMENT, "stream is NULL");
-  if (h_input) *h_input = s->h_in;
-  if (h_output) *h_output = s->h_out;
+  if (h_input) *h_input = s->h_in[s->next];
+  if (h_output) *h_output = s->h_out[s->next];
   if (d_output) *d_output = s->d_out;
   return DD_OK;
 }
@@ -364,7 +375,41 @@ dd_status dd_stream_info(const dd_stream *s, uint32_t *tail, uint64_t *device_by
 dd_status dd_stream_push(dd_stream *s, void *stream) {
   if (!s) return fail(DD_ERR_INVALID_ARGUMENT, "stream is NULL");
   DDS_CUDA(cudaSetDevice(s->device), "select device");
-  DDS_CUDA(cudaGraphLaunch(s->exec, static_cast<cudaStream_t>(stream)), "launch stream graph");
+  DDS_CUDA(cudaGraphLaunch(s->exec[s->next], static_cast<cudaStream_t>(stream)),
+           "launch stream graph");
+  s->next = (s->next + 1) % s->nbuf;
+  return DD_OK;
+}
+
+dd_status dd_stream_set_double_buffer(dd_stream *s, int enable) {
+  if (!s) return fail(DD_ERR_INVALID_ARGUMENT, "stream is NULL");
+  DDS_CUDA(cudaSetDevice(s->device), "select device");
+  const uint32_t C = s->g.one.nr_channels, S = s->g.one.nr_samples_per_batch;
+  if (enable && !s->h_in[1]) {
+    DDS_CUDA(cudaHostAlloc(&s->h_in[1], s->in_row_bytes * C, cudaHostAllocDefault),
+             "allocate staging");
+    std::memset(s->h_in[1], 0, s->in_row_bytes * C);
+    DDS_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&s->h_out[1]), (size_t)S * 4 * s->out_rows,
+                           cudaHostAllocDefault),
+             "allocate output");
+  }
+  s->nbuf = enable ? 2 : 1;
+  s->next = 0;
+  return record(s);
+}
+
+dd_status dd_stream_buffer(dd_stream *s, int index, void **h_input, float **h_output) {
+  if (!s) return fail(DD_ERR_INVALID_ARGUMENT, "stream is NULL");
+  if (index < 0 || index >= s->nbuf)
+    return fail(DD_ERR_INVALID_ARGUMENT, "buffer %d of %d", index, s->nbuf);
+  if (h_input) *h_input = s->h_in[index];
+  if (h_output) *h_output = s->h_out[index];
+  return DD_OK;
+}
+
+dd_status dd_stream_next_buffer(const dd_stream *s, int *index) {
+  if (!s || !index) return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
+  *index = s->next;
   return DD_OK;
 }
 

@@ -51,6 +51,7 @@ class BeamConfig:
     padding: int = 128
     zap_fraction: float = 0.05
     seed: int = 0
+    double_buffer: bool = False    # two pinned staging/output pairs, two batches in flight
 
     @property
     def period(self) -> float:
@@ -114,29 +115,63 @@ class Stream:
                                    C.byref(rows)))
         self.tail, self.device_bytes = tail.value, nbytes.value
         self.input_row_bytes, self.output_rows = row.value, rows.value
-        h_in, h_out, d_out = C.c_void_p(), C.c_void_p(), C.c_void_p()
-        check(lib().dd_stream_buffers(self._h, C.byref(h_in), C.byref(h_out), C.byref(d_out)))
-        n_in = cfg.channels * self.input_row_bytes
-        self.staging = np.ctypeslib.as_array(C.cast(h_in, C.POINTER(C.c_uint8)),
-                                             shape=(n_in,)).reshape(cfg.channels, -1)
-        self.output = np.ctypeslib.as_array(C.cast(h_out, C.POINTER(C.c_float)),
-                                            shape=(self.output_rows * cfg.samples,)
-                                            ).reshape(self.output_rows, cfg.samples)
-        self.dm_samples = self.output_rows * cfg.samples
+        self.nbuf, self.time_major = 1, False
+        self._map_buffers()
+        self.output = self.outputs[0]
+        self.dm_samples = self.output_rows * self.cfg.samples
+
+    def _map_buffers(self) -> None:
+        """numpy views of every pinned staging/output pair."""
+        cfg = self.cfg
+        self.stagings, self.outputs = [], []
+        for i in range(self.nbuf):
+            h_in, h_out = C.c_void_p(), C.c_void_p()
+            check(lib().dd_stream_buffer(self._h, i, C.byref(h_in), C.byref(h_out)))
+            n_in = cfg.channels * self.input_row_bytes
+            st = np.ctypeslib.as_array(C.cast(h_in, C.POINTER(C.c_uint8)), shape=(n_in,))
+            st = (st[:cfg.samples * cfg.channels].reshape(cfg.samples, cfg.channels)
+                  if self.time_major else st.reshape(cfg.channels, -1))
+            self.stagings.append(st)
+            self.outputs.append(np.ctypeslib.as_array(
+                C.cast(h_out, C.POINTER(C.c_float)),
+                shape=(self.output_rows * cfg.samples,)).reshape(self.output_rows, cfg.samples))
+
+    @property
+    def next_buffer(self) -> int:
+        i = C.c_int(0)
+        check(lib().dd_stream_next_buffer(self._h, C.byref(i)))
+        return i.value
+
+    @property
+    def staging(self) -> np.ndarray:
+        """The staging input the next push reads."""
+        return self.stagings[self.next_buffer]
+
+    def set_double_buffer(self, enable: bool = True) -> None:
+        """Two staging/output pairs used in turn: the next batch can be
+        staged while a push is in flight (dd_stream_set_double_buffer)."""
+        check(lib().dd_stream_set_double_buffer(self._h, 1 if enable else 0))
+        self.nbuf = 2 if enable else 1
+        self._map_buffers()
 
     def set_time_major(self, reverse: bool = False) -> None:
         """Take batches as time-major 8-bit blocks (file order); ``staging``
         becomes a [samples][channels] view of the same pinned buffer."""
         check(lib().dd_stream_set_time_major(self._h, 1 if reverse else 0))
-        self.staging = self.staging.reshape(-1)[:self.cfg.samples * self.cfg.channels].reshape(
-            self.cfg.samples, self.cfg.channels)
+        self.time_major = True
+        self._map_buffers()
         tail, nbytes = C.c_uint32(0), C.c_uint64(0)
         check(lib().dd_stream_info(self._h, C.byref(tail), C.byref(nbytes), None, None))
         self.device_bytes = nbytes.value
 
-    def push(self, cuda_stream) -> None:
+    def push(self, cuda_stream) -> int:
+        """Enqueue the staged batch; returns the buffer pair it uses (its
+        output lands in ``outputs[index]``, also ``output``)."""
         s = cuda_stream if isinstance(cuda_stream, int) else int(cuda_stream.cuda_stream)
+        index = self.next_buffer
         check(lib().dd_stream_push(self._h, C.c_void_p(s)))
+        self.output = self.outputs[index]
+        return index
 
     def close(self) -> None:
         if self._h:
@@ -199,6 +234,8 @@ class Server:
                                     f"beam {cfg.name} needs {need} device bytes, "
                                     f"{self.budget - self.used} of the budget are left")
         s = Stream(cfg, self.device)
+        if cfg.double_buffer:
+            s.set_double_buffer(True)
         self.used += s.device_bytes
         self.streams.append(s)
         return s
@@ -218,7 +255,9 @@ class Server:
         n = len(self.streams)
         cuda_streams = [torch.cuda.Stream(device=self.device) for _ in range(n)]
         pending = [[] for _ in range(n)]     # arrived, not yet dispatched: (t_arrival, batch)
-        inflight = [None] * n                # (event, t_arrival, batch)
+        # in flight, oldest first: (event, t_arrival, batch, buffer); up to one
+        # per staging buffer of the beam's stream (two when double-buffered)
+        inflight = [[] for _ in range(n)]
         report = ServeReport(deadline=deadline if deadline is not None
                              else max(s.cfg.period for s in self.streams),
                              time_compression=time_compression)
@@ -228,29 +267,28 @@ class Server:
             return (time.perf_counter() - t0) * time_compression
 
         def finish(b):
-            ev, ta, k = inflight[b]
+            ev, ta, k, idx = inflight[b].pop(0)
             done = now()
             report.latencies.append((done - ta) / time_compression)
             report.dm_samples += self.streams[b].dm_samples
-            inflight[b] = None
             if consumer is not None:
-                consumer(b, k, self.streams[b].output)
+                consumer(b, k, self.streams[b].outputs[idx])
 
         def dispatch(b):
-            if inflight[b] is not None or not pending[b]:
-                return
-            ta, k = pending[b].pop(0)
-            source(b, k, self.streams[b].staging)
-            self.streams[b].push(cuda_streams[b])
-            ev = torch.cuda.Event()
-            ev.record(cuda_streams[b])
-            inflight[b] = (ev, ta, k)
+            st = self.streams[b]
+            while pending[b] and len(inflight[b]) < st.nbuf:
+                ta, k = pending[b].pop(0)
+                source(b, k, st.staging)
+                idx = st.push(cuda_streams[b])
+                ev = torch.cuda.Event()
+                ev.record(cuda_streams[b])
+                inflight[b].append((ev, ta, k, idx))
 
         def poll():
             for b in range(n):
-                if inflight[b] is not None and inflight[b][0].query():
+                while inflight[b] and inflight[b][0][0].query():
                     finish(b)
-                    dispatch(b)
+                dispatch(b)
 
         for ta, b, k in schedule:
             while now() < ta:
@@ -259,10 +297,8 @@ class Server:
             pending[b].append((ta, k))
             poll()
             dispatch(b)
-        while any(x is not None for x in inflight) or any(pending):
+        while any(inflight) or any(pending):
             poll()
-            for b in range(n):
-                dispatch(b)
             time.sleep(0.0002)
         report.wall = (time.perf_counter() - t0)
         return report

@@ -476,8 +476,8 @@ dd_status dd_stream_create(dd_stream **stream, const dd_observation *obs,
                            int subband, uint32_t input_bits, uint32_t padding,
                            const float *shifts, const float *shifts_step_two,
                            const uint32_t *zapped, int device);
-/* Pinned staging input [C][S samples], pinned output [rows][S], device
- * output in the plan layout. */
+/* Pinned staging input [C][S samples] and pinned output [rows][S] of the
+ * next push, device output in the plan layout. */
 dd_status dd_stream_buffers(dd_stream *stream, void **h_input, float **h_output,
                             float **d_output);
 dd_status dd_stream_info(const dd_stream *stream, uint32_t *tail,
@@ -493,6 +493,15 @@ dd_status dd_stream_push(dd_stream *stream, void *cuda_stream);
  * the device and transposes it into the ring (dd_transpose_time_major).
  * Adds S * C device bytes.  8-bit streams only. */
 dd_status dd_stream_set_time_major(dd_stream *stream, int reverse);
+/* enable = 1: two pinned staging/output pairs used in turn (push k uses pair
+ * k % 2), so that the next batch can be staged, and the previous output read,
+ * while a push is in flight; dd_stream_buffers returns the next push's pair.
+ * A pair may be refilled once the push that used it completed. */
+dd_status dd_stream_set_double_buffer(dd_stream *stream, int enable);
+/* Pair `index` (0 or 1) of the staging input and pinned output, and the
+ * index the next push uses. */
+dd_status dd_stream_buffer(dd_stream *stream, int index, void **h_input, float **h_output);
+dd_status dd_stream_next_buffer(const dd_stream *stream, int *index);
 dd_status dd_stream_destroy(dd_stream *stream);
 
 /* ---- learned tuning: the cost model's network ---------------------------- */

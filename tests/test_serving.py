@@ -1,5 +1,7 @@
 """Real-time serving: admission by device-memory budget, and every served
 batch equal to the plain path on its window [tail | batch]."""
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -85,10 +87,11 @@ def serving_tail_step_two(stream):
 
 
 @pytest.mark.gpu
-def test_served_batches_equal_plain_path(gpu):
+@pytest.mark.parametrize("double_buffer", [False, True])
+def test_served_batches_equal_plain_path(gpu, double_buffer):
     pytest.importorskip("torch")
     server = serving.Server(budget_bytes=150 * 10**9)
-    beams = small_beams()
+    beams = [dataclasses.replace(c, double_buffer=double_buffer) for c in small_beams()]
     for cfg in beams:
         server.admit(cfg)
     nb = 4
@@ -143,5 +146,36 @@ def test_time_major_input_equals_channel_rows(gpu):
             b.push(cs)
             cs.synchronize()
             assert np.array_equal(a.output.view(np.uint32), b.output.view(np.uint32)), (cfg.name, k)
+        a.close()
+        b.close()
+
+
+@pytest.mark.gpu
+def test_double_buffered_stream_equals_single(gpu):
+    """Two pushes in flight on one CUDA stream, staged into alternating
+    pinned buffers: the same outputs as one buffer pushed batch by batch."""
+    torch = pytest.importorskip("torch")
+    cs = torch.cuda.Stream()
+    for cfg in small_beams()[:2]:
+        a, b = serving.Stream(cfg), serving.Stream(cfg)
+        b.set_double_buffer(True)
+        assert b.nbuf == 2 and b.next_buffer == 0
+        outs = []
+        for k in range(4):
+            data = batch_data(cfg, k)
+            a.staging[:, :cfg.samples] = data
+            a.push(cs)
+            cs.synchronize()
+            want = a.output.copy()
+            # b: stage batch k while batch k - 1 may still be in flight
+            b.staging[:, :cfg.samples] = data
+            idx = b.push(cs)
+            assert idx == k % 2
+            outs.append((idx, want))
+            if k % 2 == 1:
+                cs.synchronize()
+                for i, w in outs:
+                    assert np.array_equal(b.outputs[i].view(np.uint32), w.view(np.uint32)), cfg.name
+                outs = []
         a.close()
         b.close()
