@@ -88,3 +88,28 @@ def test_learned_tuner_beats_random_choice(gpu, tmp_path):
     assert fields[0] == "128" and len(fields) == 10
     assert "learned: timed 2 of" in p.stderr, p.stderr
     assert dd.readTunedDedispersionConf(str(tuned), "GB300", 128).print() == " ".join(fields[1:])
+
+
+def test_observation_shape_maps_problems_to_study_features(engine):
+    """A user problem maps onto the features the study trained on: single
+    step directly; step one as a subband shape whose DM step is the coarse
+    step / 32 and whose DM count is coarse DMs x 32 (the study's geometry)."""
+    from dedispersion_gb300 import synthetic as syn
+    obs = syn.large_observation(128)
+    sh = dd.getShifts(obs, 128)
+    s = tuning.observation_shape(obs, dd.DD_SINGLE_STEP, 8, sh)
+    assert (s.channels, s.dms, s.samples, s.subbands) == (1536, 2048, 24576, 0)
+    assert s.dm_step == pytest.approx(0.2) and s.shift0 == pytest.approx(float(sh[0]))
+    sub = syn.large_observation(128, subbands=True)
+    s1 = tuning.observation_shape(sub, dd.DD_STEP_ONE, 8, dd.getShifts(sub, 128))
+    assert (s1.subbands, s1.dms) == (32, 64 * 32) and s1.dm_step == pytest.approx(6.4 / 32)
+    assert s1.mode() == dd.DD_STEP_ONE and s.mode() == dd.DD_SINGLE_STEP
+    # the study band's default delay constant is used when shift0 is unset
+    f_default = tuning.features(tuning.Shape(1536, 2048, 24576, 8, 0, 0.2), *_first(s))
+    f_real = tuning.features(s, *_first(s))
+    assert f_default.shape == f_real.shape
+
+
+def _first(shape):
+    k = tuning.family_kernels(shape.mode(), shape.bits)[0]
+    return k.conf, k.name
