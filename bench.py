@@ -467,7 +467,7 @@ def bench_batched(torch, device: int, reps: int = 3, count: int = 40, peak_adds:
         exact &= bool(torch.equal(d_out.view(rows, -1)[:, :S], d_ref.view(rows, -1)[:, :S]))
         plan.close()
     info = batch.info()
-    shared = info.get("tile") == "shared"
+    shared = info.get("form") == "graph"
     batch.close()
     return {"value": units / t_batch, "unit": UNIT, "ms_per_batch": t_batch * 1e3,
             "plain_sequential_value": units / t_plain, "plain_sequential_ms": t_plain * 1e3,
@@ -475,7 +475,7 @@ def bench_batched(torch, device: int, reps: int = 3, count: int = 40, peak_adds:
             "adds_per_batch": adds,
             "adds_frac": adds / t_batch / peak_adds if peak_adds else None,
             ("branches" if shared else "persistent_ctas"): info["grid"],
-            "tile": info.get("tile"), "bit_exact_vs_plain": exact,
+            "form": info.get("form"), "bit_exact_vs_plain": exact,
             "launch": ("one CUDA graph: the beams' kernels on concurrent branches" if shared
                        else "one persistent kernel replayed from a CUDA graph"),
             "workload": "40 beams: 384/1536 ch, 8192-32768 samples, 512-4096 DMs, DM step "

@@ -479,9 +479,9 @@ def _stream(s) -> int:
 
 class Batch:
     """Many single-step problems (1/2/4/8-bit) in one CUDA graph recorded at
-    commit(): the problems' own kernels on concurrent branches, or one
-    persistent direct-tile kernel where a problem does not fit the
-    shared-partial-sum tile.  Device buffers are bound by add()."""
+    commit(): the problems' own default kernels on concurrent branches, or
+    (setPersistent) one persistent direct-tile kernel over all their tiles.
+    Device buffers are bound by add()."""
 
     def __init__(self, device: int = 0):
         self._h = C.c_void_p()
@@ -516,8 +516,12 @@ class Batch:
         if t.value:
             sh = C.c_int(0)
             check(lib().dd_batch_shared(self._h, C.byref(sh)))
-            info["tile"] = "shared" if sh.value else "direct"
+            info["form"] = "graph" if sh.value else "persistent"
         return info
+
+    def setPersistent(self, enable: bool = True) -> None:
+        """Commit in the persistent form (one persistent direct-tile kernel)."""
+        check(lib().dd_batch_set_persistent(self._h, 1 if enable else 0))
 
     def close(self) -> None:
         if self._h:

@@ -156,6 +156,7 @@ SIGNATURES = {
     "dd_batch_check": (C.c_int, [_P, _P]),
     "dd_batch_info": (C.c_int, [_P, _U32P, _U32P, _U32P]),
     "dd_batch_shared": (C.c_int, [_P, C.POINTER(C.c_int)]),
+    "dd_batch_set_persistent": (C.c_int, [_P, C.c_int]),
     "dd_batch_destroy": (C.c_int, [_P]),
     "dd_stream_bytes": (C.c_int, [_OBS, C.c_int, C.c_uint32, C.c_uint32, _F32P, _F32P, _U32P,
                                   C.POINTER(C.c_uint64), _U32P]),

@@ -6,20 +6,23 @@
 // that computes them all; results equal the plain path's bit for bit.
 //
 // Two forms:
-//  * every problem fits the shared-partial-sum tile (the plain path's
-//    default): the graph forks into a few branches, each launching its share
-//    of the problems' own plain kernels one after another (longest first,
+//  * graph form (the default): each problem runs its own default plan (the
+//    shared-partial-sum tile where its tables fit, else the largest direct
+//    tile that fits).  The graph forks into a few branches, each launching
+//    its share of the problems' kernels one after another (longest first,
 //    shares balanced by tile cost).  The branches run concurrently, so one
 //    problem's last partial wave of tiles overlaps the next problem's first.
-//    A persistent kernel over all the problems' tiles ran this tile 0.86-0.92x
-//    as fast per tile as the plain launches (a problem's fields then come from
-//    the kernel parameters at a runtime index, not at fixed offsets), so the
-//    batch keeps the plain kernels.
-//  * otherwise: one work list over all the problems' tiles, longest tiles
+//  * persistent form (dd_batch_set_persistent, or when some problem has no
+//    default plan): one work list over all the problems' tiles, longest tiles
 //    first (a tile's cost is its live rows), and a graph of [reset work
-//    counter, persistent kernel].  The persistent kernel runs one CTA per free
-//    slot of every SM; each CTA takes the next tile from the work counter and
-//    computes it with the direct swar8 tile routine of the plain kernel.
+//    counter, persistent kernel].  The persistent kernel runs one CTA per
+//    free slot of every SM; each CTA takes the next tile from the work
+//    counter and computes it with the direct swar8 tile routine.
+// A persistent kernel over the shared tile ran it 0.86-0.92x as fast per tile
+// as the plain launches (a problem's fields then come from the kernel
+// parameters at a runtime index, not at fixed offsets), and the persistent
+// direct kernel runs at ~0.91x of the direct plain launches, so the graph
+// form is the default.
 //
 // There is no counterpart in the reference (its test driver launches one
 // kernel per configuration and beam set, src/DedispersionTest.cpp:366-399).
@@ -99,10 +102,7 @@ __global__ void __launch_bounds__(kThreads, 2) batch_kernel(const BatchDesc B) {
   }
 }
 
-// The shared-partial-sum tile configuration of a batch: the plain path's
-// default one.
-constexpr int kSNW = 4, kSND = 4, kSTY = 16;
-// Concurrent launch chains of a shared-tile batch.
+// Concurrent launch chains of the graph form.
 constexpr uint32_t kBranches = 4;
 
 dd_status fail(dd_status code, const char *fmt, ...) {
@@ -132,9 +132,10 @@ dd_status cuda_fail(cudaError_t e, const char *what) {
 
 struct dd_batch {
   int device = 0;
-  std::vector<dd_plan *> plans;         // direct-tile plans (always built)
-  std::vector<dd_plan *> shared_plans;  // shared-tile plans (NULL: shape does not fit)
-  bool shared = false;                  // committed with the shared tile
+  std::vector<dd_plan *> plans;         // persistent-form plans (direct tile, always built)
+  std::vector<dd_plan *> shared_plans;  // each beam's default plan (NULL: none fits)
+  bool shared = false;                  // committed in the graph form
+  bool persistent = false;              // dd_batch_set_persistent
   std::vector<const void *> inputs;
   std::vector<float *> outputs;
   // committed state
@@ -297,16 +298,15 @@ dd_status dd_batch_add(dd_batch *b, const dd_observation *obs, uint32_t input_bi
     dd_plan_destroy(p);
     return st;
   }
-  // The same problem on the shared tile, if its tables fit.
-  dd_conf sconf{0, 1, (uint32_t)dd::kSharedRows, 32, kSTY, 1, 2 * kSNW, kSND,
-                (uint32_t)dd::kSharedRows};
+  // The beam's own default plan for the graph form: the shared-partial-sum
+  // tile where its tables fit, else the largest direct tile that fits.
   dd_plan *q = nullptr;
-  if (dd_plan_create(&q, obs, DD_SINGLE_STEP, input_bits, padding, &sconf, b->device) == DD_OK) {
+  if (dd_plan_create(&q, obs, DD_SINGLE_STEP, input_bits, padding, nullptr, b->device) == DD_OK) {
     bool good = dd_plan_set_shifts(q, shifts, obs->nr_channels) == DD_OK &&
                 dd_plan_set_zapped(q, zapped, obs->nr_channels) == DD_OK &&
                 dd_plan_set_beam_mapping(q, beam_mapping, (size_t)obs->nr_synthesized_beams *
                                                               lay.mapping_row_elems) == DD_OK;
-    good = good && dd::plan_ready(q) && dd::plan_family(q) == dd::kFamilyShared8;
+    good = good && dd::plan_ready(q);
     if (!good) {
       dd_plan_destroy(q);
       q = nullptr;
@@ -326,7 +326,8 @@ dd_status dd_batch_commit(dd_batch *b) {
   if (b->plans.empty()) return fail(DD_ERR_INVALID_ARGUMENT, "batch is empty");
   release(b);
   const size_t n = b->plans.size();
-  b->shared = std::all_of(b->shared_plans.begin(), b->shared_plans.end(),
+  b->shared = !b->persistent &&
+              std::all_of(b->shared_plans.begin(), b->shared_plans.end(),
                           [](dd_plan *q) { return q != nullptr; });
   DDB_CUDA(cudaSetDevice(b->device), "select device");
   if (b->shared) {
@@ -450,6 +451,13 @@ dd_status dd_batch_info(const dd_batch *b, uint32_t *problems, uint32_t *tiles, 
   if (problems) *problems = (uint32_t)b->plans.size();
   if (tiles) *tiles = b->committed ? b->total_tiles : 0;
   if (grid) *grid = b->committed ? b->grid : 0;
+  return DD_OK;
+}
+
+dd_status dd_batch_set_persistent(dd_batch *b, int enable) {
+  if (!b) return fail(DD_ERR_INVALID_ARGUMENT, "batch is NULL");
+  b->persistent = enable != 0;
+  if (b->committed) release(b);
   return DD_OK;
 }
 

@@ -427,12 +427,13 @@ dd_status dd_transpose_time_major(const void *d_src, uint32_t count, uint32_t nc
 /* No counterpart in the reference (its driver launches one kernel per beam
  * set, src/DedispersionTest.cpp:366-399).  A batch holds single-step problems
  * of 1/2/4/8-bit input, each with its own geometry, tables and device
- * buffers; committing it records one CUDA graph that computes them all.  When
- * every problem fits the shared-partial-sum tile the graph forks into a few
- * concurrent branches of the problems' own kernels (longest first, balanced
- * by tile cost); otherwise it is one work list over all the problems' tiles
- * (longest first) run by a persistent direct-tile kernel.  Results equal
- * dd_plan_run's for each problem bit for bit. */
+ * buffers; committing it records one CUDA graph that computes them all.  By
+ * default the graph forks into a few concurrent branches of the problems' own
+ * default kernels (the shared-partial-sum tile where it fits, else a direct
+ * tile; longest first, balanced by tile cost).  The persistent form is one
+ * work list over all the problems' tiles (longest first) run by a persistent
+ * direct-tile kernel.  Results equal dd_plan_run's for each problem bit for
+ * bit. */
 typedef struct dd_batch dd_batch;
 dd_status dd_batch_create(dd_batch **batch, int device);
 /* Add one single-step problem; `index` (may be NULL) receives its position.
@@ -448,13 +449,16 @@ dd_status dd_batch_commit(dd_batch *batch);
 dd_status dd_batch_run(dd_batch *batch, void *stream, int use_graph);
 /* Synchronize `stream` and report a device-side timeout. */
 dd_status dd_batch_check(dd_batch *batch, void *stream);
-/* Problems and tiles of a committed batch, and its persistent CTAs (direct
- * tile) or concurrent branches (shared tile). */
+/* Problems and tiles of a committed batch, and its concurrent branches (graph
+ * form) or persistent CTAs (persistent form). */
 dd_status dd_batch_info(const dd_batch *batch, uint32_t *problems,
                         uint32_t *tiles, uint32_t *grid);
-/* 1 if a committed batch runs the shared-partial-sum tile (every problem's
- * tables fit it), 0 if the direct tile. */
+/* 1 if a committed batch runs in the graph form (each problem's own kernel),
+ * 0 if in the persistent form. */
 dd_status dd_batch_shared(const dd_batch *batch, int *shared);
+/* enable = 1: commit in the persistent form (one persistent direct-tile
+ * kernel over all the problems' tiles).  Takes effect at the next commit. */
+dd_status dd_batch_set_persistent(dd_batch *batch, int enable);
 dd_status dd_batch_destroy(dd_batch *batch);
 
 /* ---- streams: one beam of a real-time batch stream ---------------------- */

@@ -1,8 +1,8 @@
 """Batches: uneven beams of mixed input widths in one CUDA graph launch give,
-beam by beam, exactly the plain path's output, both in the shared-tile form
-(the beams' own kernels on concurrent branches) and in the direct-tile form
-(one persistent kernel, taken when a beam does not fit the shared tile); one
-beam is also checked against the CPU oracle."""
+beam by beam, exactly the plain path's output, both in the graph form (each
+beam's own default kernel on concurrent branches, shared or direct tile) and
+in the persistent form (one persistent direct-tile kernel); beams are also
+checked against the CPU oracle."""
 import numpy as np
 import pytest
 
@@ -67,7 +67,7 @@ def test_batch_matches_plain_path(gpu, oracle):
     batch.commit()
     info = batch.info()
     assert info["problems"] == len(SHAPES) and info["tiles"] > 0
-    assert info["tile"] == "shared" and 1 <= info["grid"] <= len(SHAPES)
+    assert info["form"] == "graph" and 1 <= info["grid"] <= len(SHAPES)
     _equals_plain(batch, beams, padding)
     # one beam against the CPU oracle
     sh, obs, shifts, zapped, mapping, d_in, d_out, lay = beams[1]
@@ -80,22 +80,27 @@ def test_batch_matches_plain_path(gpu, oracle):
     batch.close()
 
 
-def test_batch_direct_tile_when_a_beam_does_not_fit(gpu, oracle):
+@pytest.mark.parametrize("persistent", [False, True])
+def test_batch_mixed_tiles_and_persistent_form(gpu, oracle, persistent):
     """A beam whose partial sums do not fit the shared tile (1 MHz channels
     from 300 MHz, DM step 0.12: ~34 samples more delay per DM step in the
-    lowest channel) moves the whole batch to the persistent direct-tile
-    kernel."""
+    lowest channel) runs its direct tile beside the others' shared tiles in
+    the graph form; the persistent form runs every beam on the persistent
+    direct-tile kernel."""
     torch = pytest.importorskip("torch")
     padding = 64
     wide = dict(obs=syn.make_observation(128, 300.0, 1.0, 81.92e-6, 512, 64, 0.0, 0.12,
                                          padding=padding), channels=128, bits=8, seed=9)
     beams = build(torch, padding, SHAPES[:3] + [wide])
     batch = dd.Batch()
+    if persistent:
+        batch.setPersistent(True)
     for sh, obs, shifts, zapped, mapping, d_in, d_out, lay in beams:
         batch.add(obs, sh["bits"], padding, shifts, zapped, mapping, d_in, d_out)
     batch.commit()
     info = batch.info()
-    assert info["tile"] == "direct" and info["grid"] > 0 and info["problems"] == 4
+    assert info["form"] == ("persistent" if persistent else "graph")
+    assert info["grid"] > 0 and info["problems"] == 4
     _equals_plain(batch, beams, padding)
     # the wide beam (a default plan falls back to a smaller direct tile) against the oracle
     sh, obs, shifts, zapped, mapping, d_in, d_out, lay = beams[3]
