@@ -131,3 +131,23 @@ def test_subband_large_matches_oracle(gpu, oracle):
     ref2 = np.zeros_like(out)
     oracle.step_two(obs.c, mapping, mid, ref2, shifts2, PADDING)
     assert np.array_equal(out.view(np.uint32), ref2.view(np.uint32))
+
+
+def test_largest_study_shape_dm_rows_match_oracle(gpu, oracle):
+    """4096 channels x 8192 DMs (the top of the tuning study's range) at
+    2048 samples, 5 % zapped: spread DM rows equal the oracle's."""
+    obs = syn.make_observation(4096, 1220.0, 300.0 / 4096, 81.92e-6, 2048, 8192, 0.0, 0.05,
+                               padding=PADDING)
+    shifts = dd.getShifts(obs, PADDING)
+    zapped = syn.zapped_mask(4096, 0.05, 11, PADDING)
+    mapping = syn.identity_mapping(obs, PADDING)
+    inp = syn.make_input(obs, 8, PADDING, seed=13, distribution="uniform")
+    out = syn.output_buffer(obs, dd.DD_SINGLE_STEP, PADDING)
+    dd.dedispersion(obs, zapped, mapping, inp, out, shifts, PADDING, 8)
+    S, row = 2048, dd.pad(2048, PADDING // 4)
+    ref = np.zeros_like(out)
+    rows = [0, 1, 63, 64, 4095, 4096, 8190, 8191]
+    for d in rows:
+        oracle.dedispersion(obs.c, zapped, mapping, inp, ref, shifts, PADDING, 8, d, d + 1)
+    got = out.reshape(-1, row)[rows, :S]
+    assert np.array_equal(got.view(np.uint32), ref.reshape(-1, row)[rows, :S].view(np.uint32))
