@@ -11,7 +11,7 @@
 // W [out][in] then b [out].
 //
 // No counterpart in the reference, whose tuner is an exhaustive sweep
-// (src/DedispersionTuning.cpp:201-437); the sweep stays the judge.
+// (src/DedispersionTuning.cpp:201-437); the sweep stays the arbiter of what is fastest.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 

@@ -13,7 +13,7 @@ cost model that times only its top candidates.
 * :class:`LearnedTuner` predicts log(time per DM-sample) of every configuration
   from shape and configuration features with the library's CUDA MLP
   (dedispersion_gb300.costmodel), then times only the top k.  The sweep stays
-  the judge; the model never touches outputs.  A trained model is saved and
+  the arbiter of what is fastest; the model never touches outputs.  A trained model is saved and
   loaded (``LearnedTuner.save`` / ``load``); on the command line
   ``-train_model model.npz`` sweeps the seeded study shapes and saves one, and
   ``-learned model.npz -top_k k`` times only the model's top k of a problem

@@ -510,7 +510,7 @@ dd_status dd_stream_destroy(dd_stream *stream);
 
 /* ---- learned tuning: the cost model's network ---------------------------- */
 /* No counterpart in the reference (its tuner is an exhaustive sweep,
- * src/DedispersionTuning.cpp:201-437, which stays the judge).  An MLP
+ * src/DedispersionTuning.cpp:201-437, which stays the arbiter of what is fastest).  An MLP
  * in -> hidden x hidden_layers -> 1 with ReLU, bf16 weights (fp32 master copy
  * for Adam), fp32 accumulation, MSE loss, trained and run by the library's own
  * CUDA kernels.  Parameters are exchanged as flat fp32 arrays: per layer
