@@ -289,12 +289,16 @@ dd_status dd_dedispersion_noalloc(const dd_observation *obs,
  * are independent. */
 typedef struct dd_plan dd_plan;
 
-/* `conf` may be NULL (dd_default_conf).  `device` is a CUDA device index. */
+/* `conf` may be NULL: the default kernel of the shape (dd_default_conf), or
+ * where its tile does not fit the shape, the direct default and then the
+ * other direct tiles of the input width, largest first.  `device` is a CUDA
+ * device index. */
 dd_status dd_plan_create(dd_plan **plan, const dd_observation *obs,
                          dd_mode mode, uint32_t input_bits, uint32_t padding,
                          const dd_conf *conf, int device);
-/* Host tables, copied to the device.  Shifts are required; the zapped mask
- * (nonzero = skip) defaults to none zapped, the beam mapping to identity. */
+/* Host tables, copied to the device when the plan is first used (run,
+ * timing, dd_plan_adds).  Shifts are required; the zapped mask (nonzero =
+ * skip) defaults to none zapped, the beam mapping to identity. */
 dd_status dd_plan_set_shifts(dd_plan *plan, const float *shifts, size_t n);
 dd_status dd_plan_set_zapped(dd_plan *plan, const uint32_t *zapped, size_t n);
 dd_status dd_plan_set_beam_mapping(dd_plan *plan, const uint32_t *mapping,
