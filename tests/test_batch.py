@@ -110,3 +110,23 @@ def test_batch_mixed_tiles_and_persistent_form(gpu, oracle, persistent):
     got = d_out.cpu().numpy().reshape(-1, lay.output_row_elems)[:, :S]
     np.testing.assert_array_equal(got, ref.reshape(-1, lay.output_row_elems)[:, :S])
     batch.close()
+
+
+def test_batch_of_many_small_beams(gpu):
+    """200 small beams (more than any fixed parameter space would hold) in
+    one graph: every beam equals its plain run."""
+    torch = pytest.importorskip("torch")
+    padding = 64
+    rng = np.random.default_rng(5)
+    shapes = [dict(channels=int(rng.choice([32, 64, 96])), bandwidth=2.0,
+                   samples=int(rng.integers(64, 512)), dms=int(rng.integers(1, 24)),
+                   dm_step=float(rng.uniform(0.1, 0.5)), bits=int(rng.choice([2, 4, 8])),
+                   seed=1000 + i) for i in range(200)]
+    beams = build(torch, padding, shapes)
+    batch = dd.Batch()
+    for sh, obs, shifts, zapped, mapping, d_in, d_out, lay in beams:
+        batch.add(obs, sh["bits"], padding, shifts, zapped, mapping, d_in, d_out)
+    batch.commit()
+    assert batch.info()["problems"] == 200 and batch.info()["form"] == "graph"
+    _equals_plain(batch, beams, padding)
+    batch.close()

@@ -179,3 +179,32 @@ def test_double_buffered_stream_equals_single(gpu):
                 outs = []
         a.close()
         b.close()
+
+
+@pytest.mark.gpu
+def test_time_major_double_buffered_stream(gpu):
+    """File-order blocks into alternating staging buffers, two pushes in
+    flight: the same outputs as channel rows pushed one at a time."""
+    torch = pytest.importorskip("torch")
+    cs = torch.cuda.Stream()
+    cfg = small_beams()[1]  # 8-bit subband
+    a, b = serving.Stream(cfg), serving.Stream(cfg)
+    b.set_time_major(reverse=True)
+    b.set_double_buffer(True)
+    assert b.staging.shape == (cfg.samples, cfg.channels)
+    want, got_idx = [], []
+    for k in range(4):
+        data = batch_data(cfg, k)
+        a.staging[:, :cfg.samples] = data
+        a.push(cs)
+        cs.synchronize()
+        want.append(a.output.copy())
+        b.staging[:] = data[::-1].T
+        got_idx.append(b.push(cs))
+        if k % 2 == 1:
+            cs.synchronize()
+            for i, w in zip(got_idx, want):
+                assert np.array_equal(b.outputs[i].view(np.uint32), w.view(np.uint32))
+            want, got_idx = [], []
+    a.close()
+    b.close()
