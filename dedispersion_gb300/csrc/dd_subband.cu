@@ -9,9 +9,8 @@
 // 8-bit input), the intermediate is packed: one 32-bit word per sample holds
 // the exact sums of two coarse DMs (ProblemDesc::packed).  That halves its
 // bytes (101 MB instead of 202 MB at 1536 channels, 32 subbands, 64 coarse
-// DMs, 24649 samples, small enough to stay largely in the 129 MB L2 between
-// the steps), and step two's pair tile adds both coarse DMs with one load and
-// one add.
+// DMs, 24649 samples), so the round trip through device memory halves too,
+// and step two's pair tile adds both coarse DMs with one load and one add.
 // Sums are integers below 2^24 either way, so the output equals the
 // reference's float step one followed by its float step two bit for bit.
 // Otherwise (16-bit or float input, or wider subbands) the pipeline runs the
