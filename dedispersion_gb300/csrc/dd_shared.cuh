@@ -25,7 +25,8 @@
 //
 // A pipeline stage holds up to kSubMax subgroups (kStageRows rows).  Per
 // stage: the rows and the stage table arrive by 16-byte asynchronous copies
-// (every thread copies a share, completion counted on the slot's mbarrier)
+// (the last four warps issue them, every thread's arrival counted on the
+// slot's mbarrier)
 // in one of kSharedSlots slots; the CTA expands them into four byte-shifted copies
 // (any window read is one aligned 32-bit load); warps run the chains of
 // (subgroup, 31-group chunk) work items, writing each series in two copies
@@ -135,30 +136,41 @@ __device__ __forceinline__ uint4 shared_row_info(const ProblemDesc &P, uint32_t 
   return __ldg(P.stage_rows + ((size_t)g * P.stage_count + stage) * kStageRows + r);
 }
 
+// The last kCopyThreads threads of the CTA (four warps) stage the rows and
+// tables; the others go straight on to their partial sums.  Issuing a stage's
+// ~1100 asynchronous copies stalls the issuing warps for about a thousand
+// cycles (outstanding global requests), and the last warps of a stage have
+// the fewest phase-A items.
+constexpr int kCopyThreads = 128;
+constexpr uint32_t kCopyPerRow = kCopyThreads / kStageRows;  // threads per row slot
+
 // Copies one stage into `slot` with 16-byte asynchronous copies (the
-// vectorised staging path; one bulk copy per ~500-byte row costs more): 16
-// threads per row slot, thread tid also copies 16 bytes of the stage table,
-// then every thread arrives on the slot's mbarrier when its copies land.
-// `info` is the thread's row slot (row tid / 16).
+// vectorised staging path; one bulk copy per ~500-byte row costs more):
+// copy thread `ctid` (0 .. kCopyThreads - 1, negative for the other threads)
+// copies a share of row slot ctid / kCopyPerRow and of the stage table, then
+// every thread arrives on the slot's mbarrier when its copies land.  `info`
+// is the copy thread's row slot.
 __device__ __forceinline__ void shared_copy(const ProblemDesc &P, const uint4 &info,
                                             uint32_t slot, uint32_t t0, const SharedLayout &L,
-                                            uint8_t *smem, int tid) {
-  const uint32_t r = (uint32_t)tid >> 4, c0 = (uint32_t)tid & 15u;
-  if ((info.z & kRowPresent) && P.tma) {
-    const uint32_t a = align_samples(P.bits);
-    const uint32_t ws = (t0 + (info.z & ~kRowPresent)) & ~(a - 1u);
-    const uint64_t boff = (uint64_t)ws * P.bits / 8u;
-    const uint64_t avail = P.row_bytes - boff;
-    const uint8_t *src = P.in + (((uint64_t)info.y << 32) | info.x) + boff;
-    const uint32_t dst = smem_addr(smem + L.off_raw + (slot * kStageRows + r) * L.raw_bytes);
-    for (uint32_t b = 16u * c0; b < L.raw_bytes; b += 256u) {
-      const uint32_t n = avail > b ? (avail - b < 16u ? (uint32_t)(avail - b) : 16u) : 0u;
-      cp_async16(dst + b, n ? src + b : src, n);
+                                            uint8_t *smem, int ctid) {
+  if (ctid >= 0) {
+    const uint32_t r = (uint32_t)ctid / kCopyPerRow, c0 = (uint32_t)ctid % kCopyPerRow;
+    if ((info.z & kRowPresent) && P.tma) {
+      const uint32_t a = align_samples(P.bits);
+      const uint32_t ws = (t0 + (info.z & ~kRowPresent)) & ~(a - 1u);
+      const uint64_t boff = (uint64_t)ws * P.bits / 8u;
+      const uint64_t avail = P.row_bytes - boff;
+      const uint8_t *src = P.in + (((uint64_t)info.y << 32) | info.x) + boff;
+      const uint32_t dst = smem_addr(smem + L.off_raw + (slot * kStageRows + r) * L.raw_bytes);
+      for (uint32_t b = 16u * c0; b < L.raw_bytes; b += 16u * kCopyPerRow) {
+        const uint32_t n = avail > b ? (avail - b < 16u ? (uint32_t)(avail - b) : 16u) : 0u;
+        cp_async16(dst + b, n ? src + b : src, n);
+      }
     }
+    const uint32_t tdst = smem_addr(smem + L.off_table + slot * P.table_bytes);
+    for (uint32_t b = 16u * (uint32_t)ctid; b < P.table_bytes; b += 16u * kCopyThreads)
+      cp_async16(tdst + b, P.pool + info.w + b / 2u, 16u);
   }
-  if (16u * (uint32_t)tid < P.table_bytes)
-    cp_async16(smem_addr(smem + L.off_table + slot * P.table_bytes) + 16u * tid,
-               P.pool + info.w + 8u * tid, 16u);
   cp_async_arrive(reinterpret_cast<uint64_t *>(smem) + slot);
 }
 
@@ -168,7 +180,8 @@ template <int NW, int ND, int TY>
 __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_index,
                                              const GroupDesc &G, uint32_t dtile, uint32_t ttile,
                                              uint8_t *smem, const SharedLayout &L, uint32_t &sc) {
-  static_assert(32 * TY == 16 * kStageRows, "16 threads per row slot");
+  static_assert(32 * TY >= kCopyThreads && kCopyThreads % kStageRows == 0,
+                "copy threads: whole warps, equal shares of the row slots");
   constexpr int kTileT = 64 * NW;
   constexpr int kTileD = TY * ND;
   constexpr uint32_t kAhead = kSharedSlots - 1;
@@ -186,17 +199,18 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
   const uint32_t copy_s = smem_addr(copy);
   const uint32_t part_s = smem_addr(smem + L.off_part);
 
-  // Every thread copies a share of each stage; `next` is its row slot of the
-  // next stage to copy, loaded one stage ahead.
-  const uint32_t myrow = (uint32_t)tid >> 4;
+  // The copy threads stage every stage; `next` is a copy thread's row slot of
+  // the next stage to copy, loaded one stage ahead.
+  const int ctid = tid - (32 * TY - kCopyThreads);
+  const uint32_t myrow = ctid >= 0 ? (uint32_t)ctid / kCopyPerRow : 0u;
   {
     const uint32_t pro = nst < kAhead ? nst : kAhead;
     for (uint32_t s = 0; s < pro; ++s)
-      shared_copy(P, shared_row_info(P, g_index, sbeg + s, myrow), (sc + s) % kSharedSlots, t0,
-                  L, smem, tid);
+      shared_copy(P, ctid >= 0 ? shared_row_info(P, g_index, sbeg + s, myrow) : uint4{},
+                  (sc + s) % kSharedSlots, t0, L, smem, ctid);
   }
   uint4 next = make_uint4(0, 0, 0, 0);
-  if (kAhead < nst) next = shared_row_info(P, g_index, sbeg + kAhead, myrow);
+  if (ctid >= 0 && kAhead < nst) next = shared_row_info(P, g_index, sbeg + kAhead, myrow);
 
   uint32_t acc[ND][NW], tot[ND][NW][2];
 #pragma unroll
@@ -283,8 +297,9 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
     if (__syncthreads_or(!ok)) return abort(s);
     // Every thread is past the previous stage: its slot takes stage s + kAhead.
     if (s + kAhead < nst) {
-      shared_copy(P, next, (gs + kAhead) % kSharedSlots, t0, L, smem, tid);
-      if (s + kAhead + 1 < nst) next = shared_row_info(P, g_index, sbeg + s + kAhead + 1, myrow);
+      shared_copy(P, next, (gs + kAhead) % kSharedSlots, t0, L, smem, ctid);
+      if (ctid >= 0 && s + kAhead + 1 < nst)
+        next = shared_row_info(P, g_index, sbeg + s + kAhead + 1, myrow);
     }
 
     // Phase A: item = (subgroup, chunk of 31 groups of 4 samples); lane 31
