@@ -198,6 +198,10 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
   uint32_t *copy = reinterpret_cast<uint32_t *>(smem + L.off_copy);
   const uint32_t copy_s = smem_addr(copy);
   const uint32_t part_s = smem_addr(smem + L.off_part);
+  const uint32_t sbase = smem_addr(smem);
+  // Phase B reads the series with plain loads (the compiler schedules them
+  // more freely than volatile ones; measured 2 % faster).
+  auto ldc = [&](uint32_t x) { return *reinterpret_cast<const uint32_t *>(smem + (x - sbase)); };
 
   // The copy threads stage every stage; `next` is a copy thread's row slot of
   // the next stage to copy, loaded one stage ahead.
@@ -271,19 +275,7 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
         const uint32_t xw = ((t0 + bm) & (a - 1u)) >> 2;
         const uint8_t *row = rs + r * L.raw_bytes;
         uint32_t *dst = copy + r * 4u * cw;
-        const uint32_t k0 = 2u * (tx + 32u * (TY >= kStageRows ? ty / kStageRows : 0));
-        for (uint32_t kk = k0; kk < cw; kk += 64u * kRowWarps) {
-          uint32_t w0, w1, w2;
-          if (P.bits == 8) {
-            const uint32_t *r32 = reinterpret_cast<const uint32_t *>(row) + xw + kk;
-            w0 = r32[0];
-            w1 = r32[1];
-            w2 = r32[2];
-          } else {
-            w0 = expand_word(row, xw + kk, P.bits);
-            w1 = expand_word(row, xw + kk + 1, P.bits);
-            w2 = expand_word(row, xw + kk + 2, P.bits);
-          }
+        auto put = [&](uint32_t kk, uint32_t w0, uint32_t w1, uint32_t w2) {
           *reinterpret_cast<uint2 *>(dst + kk) = make_uint2(w0, w1);
           *reinterpret_cast<uint2 *>(dst + cw + kk) =
               make_uint2(__funnelshift_r(w0, w1, 8), __funnelshift_r(w1, w2, 8));
@@ -291,6 +283,17 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
               make_uint2(__funnelshift_r(w0, w1, 16), __funnelshift_r(w1, w2, 16));
           *reinterpret_cast<uint2 *>(dst + 3 * cw + kk) =
               make_uint2(__funnelshift_r(w0, w1, 24), __funnelshift_r(w1, w2, 24));
+        };
+        const uint32_t wr = TY >= kStageRows ? ty / kStageRows : 0;
+        if (P.bits == 8) {
+          for (uint32_t kk = 2u * (tx + 32u * wr); kk < cw; kk += 64u * kRowWarps) {
+            const uint32_t *r32 = reinterpret_cast<const uint32_t *>(row) + xw + kk;
+            put(kk, r32[0], r32[1], r32[2]);
+          }
+        } else {
+          for (uint32_t kk = 2u * (tx + 32u * wr); kk < cw; kk += 64u * kRowWarps)
+            put(kk, expand_word(row, xw + kk, P.bits), expand_word(row, xw + kk + 1, P.bits),
+                expand_word(row, xw + kk + 2, P.bits));
         }
       }
     }
@@ -345,12 +348,6 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
         sts_v2_if(on, pg + dst + 4u * psw, __byte_perm(lo, hi, 0x5432),
                   __byte_perm(hi, nlo, 0x5432));
       };
-      auto step = [&](const uint4 &u, uint32_t &lo, uint32_t &hi) {
-        const uint32_t wo = lds_u32(gb + u.x);
-        const uint32_t wn = lds_u32(gb + u.y);
-        lo = lo - __byte_perm(wo, 0, 0x4140) + __byte_perm(wn, 0, 0x4140);
-        hi = hi - __byte_perm(wo, 0, 0x4342) + __byte_perm(wn, 0, 0x4342);
-      };
       rows(prog + 4, loA, hiA);
       if (hasB) rows(prog + 12, loB, hiB);
       store(hdr.z, 1u, loA, hiA);
@@ -359,12 +356,32 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
       // halves to the same length with no-op micro-ops.
       const uint4 *ua = reinterpret_cast<const uint4 *>(prog + 20);
       const uint4 *ub = ua + nA;
-      for (uint32_t i = 0; i < nA; ++i) {
-        const uint4 a = ua[i], b = ub[i];
-        step(a, loA, hiA);
-        step(b, loB, hiB);
-        store(a.z, a.w, loA, hiA);
-        store(b.z, b.w, loB, hiB);
+      auto apply = [&](uint32_t wo, uint32_t wn, uint32_t &lo, uint32_t &hi) {
+        lo = lo - __byte_perm(wo, 0, 0x4140) + __byte_perm(wn, 0, 0x4140);
+        hi = hi - __byte_perm(wo, 0, 0x4342) + __byte_perm(wn, 0, 0x4342);
+      };
+      if (nA) {
+        // Software pipeline: the row words of step i + 1 and the micro-ops of
+        // step i + 2 are loaded before step i's stores (the shared-memory
+        // accesses are volatile: they issue in source order).  Row addresses
+        // are formed by IMAD, on the FMA pipe, leaving the integer ALU pipe
+        // to the unpacking and the adds.
+        uint4 a = ua[0], b = ub[0];
+        uint32_t oa = lds_u32(mad_lo(a.x, one, gb)), na = lds_u32(mad_lo(a.y, one, gb));
+        uint32_t ob = lds_u32(mad_lo(b.x, one, gb)), nb = lds_u32(mad_lo(b.y, one, gb));
+        uint4 an = ua[nA > 1 ? 1 : 0], bn = ub[nA > 1 ? 1 : 0];
+        for (uint32_t i = 0; i < nA; ++i) {
+          const uint32_t oa1 = lds_u32(mad_lo(an.x, one, gb)), na1 = lds_u32(mad_lo(an.y, one, gb));
+          const uint32_t ob1 = lds_u32(mad_lo(bn.x, one, gb)), nb1 = lds_u32(mad_lo(bn.y, one, gb));
+          const uint32_t i2 = i + 2 < nA ? i + 2 : nA - 1;
+          const uint4 an2 = ua[i2], bn2 = ub[i2];
+          apply(oa, na, loA, hiA);
+          apply(ob, nb, loB, hiB);
+          store(a.z, a.w, loA, hiA);
+          store(b.z, b.w, loB, hiB);
+          a = an; b = bn; an = an2; bn = bn2;
+          oa = oa1; na = na1; ob = ob1; nb = nb1;
+        }
       }
     }
     __syncthreads();
@@ -383,8 +400,8 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
       const uint32_t a0 = pb + oo.x, a1 = pb + oo.y, a2 = pb + oo.z, a3 = pb + oo.w;
 #pragma unroll
       for (int i = 0; i < NW; ++i) {
-        acc[j][i] += lds_u32(a0 + 128u * i) + lds_u32(a1 + 128u * i);
-        acc[j][i] += lds_u32(a2 + 128u * i) + lds_u32(a3 + 128u * i);
+        acc[j][i] += ldc(a0 + 128u * i) + ldc(a1 + 128u * i);
+        acc[j][i] += ldc(a2 + 128u * i) + ldc(a3 + 128u * i);
       }
     }
   }
