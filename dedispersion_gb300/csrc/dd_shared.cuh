@@ -49,7 +49,8 @@ constexpr int kStageRows = kSubMax * kSharedRows;       // rows per stage
 constexpr uint32_t kLaneSeries = 32;                    // series per 16-bit lane (32 * 2040 < 2^16)
 constexpr uint32_t kItemsMax = 32;                      // phase-A items per stage
 // Stage table (in shared memory; u16 units unless noted):
-//   [0] nsub [1] nrows [2] nitems [3..7] 0
+//   [0] nsub [1] nrows [2] nitems [3 + k] copy words of subgroup k's rows
+//   (even, <= cw) [7] 0
 //   [8 + 4k] bmin_k lo, [+1] bmin_k hi, [+2] first row of k, [+3] program of k
 //   [kTabItems ..)     items: subgroup << 8 | chunk
 //   [kTabSeries ..)    u32: per DM of the tile, kSubMax series byte offsets
@@ -273,6 +274,7 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
         const uint32_t k = (r >= tb[8 + 4 + 2]) + (r >= tb[8 + 8 + 2]) + (r >= tb[8 + 12 + 2]);
         const uint32_t bm = tb[8 + 4 * k] | ((uint32_t)tb[8 + 4 * k + 1] << 16);
         const uint32_t xw = ((t0 + bm) & (a - 1u)) >> 2;
+        const uint32_t cwk = tb[3 + k] < cw ? tb[3 + k] : cw;  // words phase A reads
         const uint8_t *row = rs + r * L.raw_bytes;
         uint32_t *dst = copy + r * 4u * cw;
         auto put = [&](uint32_t kk, uint32_t w0, uint32_t w1, uint32_t w2) {
@@ -286,12 +288,12 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
         };
         const uint32_t wr = TY >= kStageRows ? ty / kStageRows : 0;
         if (P.bits == 8) {
-          for (uint32_t kk = 2u * (tx + 32u * wr); kk < cw; kk += 64u * kRowWarps) {
+          for (uint32_t kk = 2u * (tx + 32u * wr); kk < cwk; kk += 64u * kRowWarps) {
             const uint32_t *r32 = reinterpret_cast<const uint32_t *>(row) + xw + kk;
             put(kk, r32[0], r32[1], r32[2]);
           }
         } else {
-          for (uint32_t kk = 2u * (tx + 32u * wr); kk < cw; kk += 64u * kRowWarps)
+          for (uint32_t kk = 2u * (tx + 32u * wr); kk < cwk; kk += 64u * kRowWarps)
             put(kk, expand_word(row, xw + kk, P.bits), expand_word(row, xw + kk + 1, P.bits),
                 expand_word(row, xw + kk + 2, P.bits));
         }

@@ -282,6 +282,9 @@ std::string build_shared_tables(const KernelInfo &k, const std::vector<float> &r
         }
         const Sub &s = subs[i + q];
         const uint32_t ng = ceil_div(s.spread + T + 2, 4) + 1;
+        // copy words phase A reads in each of the subgroup's rows: rel >> 2 + g
+        // for g < ng (even: the expansion writes word pairs)
+        tb[3 + q] = (uint16_t)std::min<uint32_t>(((s.maxrel >> 2) + ng + 1) & ~1u, S.cw);
         tb[8 + 4 * q + 0] = (uint16_t)(s.bmin & 0xFFFFu);
         tb[8 + 4 * q + 1] = (uint16_t)(s.bmin >> 16);
         tb[8 + 4 * q + 2] = (uint16_t)rstart;

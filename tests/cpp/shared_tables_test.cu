@@ -110,6 +110,7 @@ int main(int argc, char **argv) {
           // expansion
           std::fill(copy.begin(), copy.end(), 0xA5A5A5A5u);
           std::fill(copy.begin() + zrow, copy.end(), 0u);
+          uint32_t row_words[kStageRows] = {0};  // words the kernel expands per row
           for (uint32_t r = 0; r < nrows; r++) {
             const uint32_t q = (r >= T16(8 + 4 + 2)) + (r >= T16(8 + 8 + 2)) + (r >= T16(8 + 12 + 2));
             if (q != st.row_sub[r]) return fail("row subgroup", s, r, q);
@@ -118,8 +119,11 @@ int main(int argc, char **argv) {
             const uint64_t ws = (t0 + bm) / 16 * 16;
             const uint32_t x0 = t0 + bm - (uint32_t)ws;
             if (x0 + 4 * cw + 8 > win) return fail("raw window", s, x0, win);
+            const uint32_t cwk = std::min<uint32_t>(T16(3 + q), cw);
+            if (cwk % 2) return fail("odd copy width", s, q, cwk);
+            row_words[r] = cwk;
             for (uint32_t m = 0; m < 4; m++)
-              for (uint32_t kk = 0; kk < cw; kk++) {
+              for (uint32_t kk = 0; kk < cwk; kk++) {
                 uint32_t w = 0;
                 for (uint32_t i = 0; i < 4; i++)
                   w |= sample(st.row_first + r, ws, ws + x0 + 4 * kk + m + i) << (8 * i);
@@ -140,6 +144,7 @@ int main(int argc, char **argv) {
             if ((size_t)off + g >= copy.size()) return false;
             if ((off % cw) + g >= cw) return false;  // stays in its copy of its row
             if (off / (4 * cw) >= nrows) return false;
+            if ((off % cw) + g >= row_words[off / (4 * cw)]) return false;  // expanded words only
             w = copy[off + g];
             return true;
           };
