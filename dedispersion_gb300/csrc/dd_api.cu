@@ -517,9 +517,6 @@ dd_status rebuild(dd_plan *p) {
   if (p->use_delay_tables) {
     if (p->delay_rel.size() > p->cap_delay_rel) {
       if (p->d_delay_rel) cudaFree(p->d_delay_rel);
-    if (p->d_stage_rows) cudaFree(p->d_stage_rows);
-    if (p->d_tile_stage) cudaFree(p->d_tile_stage);
-    if (p->d_pool) cudaFree(p->d_pool);
       p->d_delay_rel = nullptr;
       DD_CUDA(cudaMalloc(&p->d_delay_rel, p->delay_rel.size() * sizeof(uint16_t)),
               "allocate delay table");
@@ -581,9 +578,34 @@ dd_status rebuild(dd_plan *p) {
 // that tile does not fit (its tables or window outgrow shared memory) the
 // direct default, then the other direct tiles of the same width, largest
 // (samples x DMs x rows per stage) first.
+// The shared-partial-sum tile pays for its stage machinery (row expansion,
+// chains, barriers) per executed add; the direct tile does one packed add
+// per direct-sum add.  Timed on the 40 uneven beams of the batched
+// benchmark (384 and 1536 channels, 2/4/8-bit, DM steps 0.1-0.47): the
+// shared tile is faster while its executed adds stay below ~0.34 of the
+// direct sum (ratios 0.20-0.33: 0.46-0.90 of the direct time) and slower
+// above (0.35-0.48: 1.02-2.12 of it).
+constexpr double kSharedMaxAddsRatio = 0.34;
+
+bool shared_worth_it(const dd_plan *p) {
+  const uint64_t rows = p->nr_groups ? p->entries.size() / p->nr_groups : 0;
+  const double direct = (double)rows * p->obs.nr_dms * p->kinfo->tile_t;
+  const double shared = (double)(p->shared.adds_partial + p->shared.adds_series);
+  return direct <= 0 || shared <= kSharedMaxAddsRatio * direct;
+}
+
 dd_status rebuild_auto(dd_plan *p) {
   if (p->auto_kernel) p->kinfo = default_kernel(p->mode, p->bits, true);
   dd_status st = rebuild(p);
+  if (st == DD_OK && p->auto_kernel && p->kinfo->family == dd::kFamilyShared8 &&
+      !shared_worth_it(p)) {
+    const dd::KernelInfo *shared = p->kinfo;
+    p->kinfo = default_kernel(p->mode, p->bits, false);
+    st = rebuild(p);
+    if (st == DD_OK) return st;
+    p->kinfo = shared;  // the direct tile does not fit: keep the shared one
+    return rebuild(p);
+  }
   if (st != DD_ERR_UNSUPPORTED || !p->auto_kernel) return st;
   const std::string first = g_error;
   const dd::KernelInfo *direct = default_kernel(p->mode, p->bits, false);

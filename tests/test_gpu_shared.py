@@ -165,10 +165,9 @@ def test_overlapped_runs_equal_serial_runs(gpu, family):
     two consecutive runs write the same output buffer; shared and direct
     tiles."""
     torch = pytest.importorskip("torch")
-    kidx = None
-    if family == "direct":
-        kidx = next(k.index for k in dd.kernels()
-                    if k.elem_bits == 8 and k.conf.getNrItemsD2() != 8)
+    want_d2 = 8 if family == "shared" else 1
+    kidx = next(k.index for k in dd.kernels()
+                if k.elem_bits == 8 and k.conf.getNrItemsD2() == want_d2)
     a = single_case(C=512, D=512, S=16384, bits=8, padding=128, zap=0.05, seed=41, dist="uniform")
     b = single_case(C=512, D=512, S=16384, bits=8, padding=128, zap=0.05, seed=42, dist="uniform")
     assert np.array_equal(a.shifts, b.shifts)
@@ -199,3 +198,41 @@ def test_overlapped_runs_equal_serial_runs(gpu, family):
     assert torch.equal(same, want_b) and torch.equal(out_a, want_a) and torch.equal(out_b, want_b)
     for p in (serial, ov):
         p.close()
+
+
+@pytest.mark.parametrize("channels,bandwidth,step,want_shared", [
+    (1536, 0.1953125, 0.2, True),     # executed adds ~0.23 of the direct sum
+    (384, 0.78125, 0.467, False),     # ~0.48: the direct tile is twice as fast
+])
+def test_default_tile_follows_the_sharing_gain(gpu, channels, bandwidth, step, want_shared):
+    """The default single-step plan keeps the shared tile only while its
+    executed adds stay below 0.34 of the direct sum; either way the output is
+    the direct sum (equal to the explicitly chosen other family's)."""
+    torch = pytest.importorskip("torch")
+    obs = syn.make_observation(channels, 1220.0, bandwidth, 81.92e-6, 4096, 1024, 0.0, step,
+                               padding=128)
+    shifts = dd.getShifts(obs, 128)
+    zapped = syn.zapped_mask(channels, 0.05, 5, 128)
+    mapping = syn.identity_mapping(obs, 128)
+    d_in = syn.device_uniform_input(torch, obs, 8, 128, 9)
+    lay = dd.layout(obs, dd.DD_SINGLE_STEP, 8, 128)
+    shared_idx = next(k.index for k in dd.kernels()
+                      if k.elem_bits == 8 and k.conf.getNrItemsD2() == 8)
+    outs, confs, adds = [], [], []
+    for kidx in (None, shared_idx):
+        p = dd.Plan(obs, dd.DD_SINGLE_STEP, 8, 128, kernel=kidx)
+        p.setShifts(shifts)
+        p.setZappedChannels(zapped)
+        p.setBeamMapping(mapping)
+        d_out = torch.zeros(lay.output_bytes // 4, dtype=torch.float32, device="cuda")
+        p.run(d_in, d_out)
+        p.check()
+        outs.append(d_out.cpu().numpy())
+        confs.append(p.conf())
+        adds.append(p.adds())
+        p.close()
+    live = int((np.asarray(zapped)[:channels] == 0).sum())
+    ratio = adds[1] / (live * 1024 * obs.getNrSamplesPerBatch())
+    assert (ratio < 0.34) == want_shared, ratio
+    assert (confs[0].getNrItemsD2() == 8) == want_shared
+    np.testing.assert_array_equal(outs[0].view(np.uint32), outs[1].view(np.uint32))
