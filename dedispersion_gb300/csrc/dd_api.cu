@@ -573,11 +573,10 @@ dd_status rebuild(dd_plan *p) {
 }
 
 // rebuild(), and for plans created without a configuration: the default
-// shared kernel, else (a shape it cannot take) the default direct kernel.
-// A plan without a configuration runs the default kernel of its shape; where
-// that tile does not fit (its tables or window outgrow shared memory) the
-// direct default, then the other direct tiles of the same width, largest
-// (samples x DMs x rows per stage) first.
+// shared kernel while it saves enough adds (shared_worth_it), else the
+// default direct kernel.  Where a tile does not fit (its tables or window
+// outgrow shared memory): the direct default, then the other direct tiles of
+// the same width, largest (samples x DMs x rows per stage) first.
 // The shared-partial-sum tile pays for its stage machinery (row expansion,
 // chains, barriers) per executed add; the direct tile does one packed add
 // per direct-sum add.  Timed on the 40 uneven beams of the batched

@@ -7,8 +7,8 @@
 //
 // Two forms:
 //  * graph form (the default): each problem runs its own default plan (the
-//    shared-partial-sum tile where its tables fit, else the largest direct
-//    tile that fits).  The graph forks into a few branches, each launching
+//    tile dd_plan_create picks without a configuration: shared partial sums
+//    where they fit and save enough adds, else a direct tile).  The graph forks into a few branches, each launching
 //    its share of the problems' kernels one after another (longest first,
 //    shares balanced by tile cost).  The branches run concurrently, so one
 //    problem's last partial wave of tiles overlaps the next problem's first.
@@ -298,8 +298,8 @@ dd_status dd_batch_add(dd_batch *b, const dd_observation *obs, uint32_t input_bi
     dd_plan_destroy(p);
     return st;
   }
-  // The beam's own default plan for the graph form: the shared-partial-sum
-  // tile where its tables fit, else the largest direct tile that fits.
+  // The beam's own default plan for the graph form (dd_plan_create without a
+  // configuration).
   dd_plan *q = nullptr;
   if (dd_plan_create(&q, obs, DD_SINGLE_STEP, input_bits, padding, nullptr, b->device) == DD_OK) {
     bool good = dd_plan_set_shifts(q, shifts, obs->nr_channels) == DD_OK &&

@@ -291,8 +291,10 @@ typedef struct dd_plan dd_plan;
 
 /* `conf` may be NULL: the default kernel of the shape (dd_default_conf), or
  * where its tile does not fit the shape, the direct default and then the
- * other direct tiles of the input width, largest first.  `device` is a CUDA
- * device index. */
+ * other direct tiles of the input width, largest first.  For single-step
+ * 1-8-bit input the default is the shared-partial-sum tile while its
+ * executed adds stay below 0.34 of the direct sum, else the direct default
+ * (measured crossover).  `device` is a CUDA device index. */
 dd_status dd_plan_create(dd_plan **plan, const dd_observation *obs,
                          dd_mode mode, uint32_t input_bits, uint32_t padding,
                          const dd_conf *conf, int device);
@@ -433,8 +435,8 @@ dd_status dd_transpose_time_major(const void *d_src, uint32_t count, uint32_t nc
  * of 1/2/4/8-bit input, each with its own geometry, tables and device
  * buffers; committing it records one CUDA graph that computes them all.  By
  * default the graph forks into a few concurrent branches of the problems' own
- * default kernels (the shared-partial-sum tile where it fits, else a direct
- * tile; longest first, balanced by tile cost).  The persistent form is one
+ * default kernels (as dd_plan_create with no configuration picks them;
+ * longest first, balanced by tile cost).  The persistent form is one
  * work list over all the problems' tiles (longest first) run by a persistent
  * direct-tile kernel.  Results equal dd_plan_run's for each problem bit for
  * bit. */
