@@ -75,6 +75,10 @@ def parse():
     ap.add_argument("--kernel-only", action="store_true",
                     help="run only the warm-up and timed kernel launches (the command ncu "
                          "captures); prints the device-resident figure alone")
+    ap.add_argument("--subband-only", type=int, default=None, metavar="CHUNKS",
+                    help="run only the subband pipeline, --warmup + --steps runs with "
+                         "dd_subband_set_chunks(CHUNKS) (the command ncu captures for the "
+                         "intermediate's DRAM traffic); prints its time per batch")
     return ap.parse_args()
 
 
@@ -327,6 +331,45 @@ def bench_float(torch, device: int, steps: int, peak_adds: float):
             "workload": "1536 ch x 2048 DM x 24576 samples, float32 N(128, 20), 5% zapped"}
 
 
+def subband_inputs(torch, device: int):
+    """The subband workload's pipeline and device buffers (4 rotating inputs)."""
+    import dedispersion_gb300 as dd
+    from dedispersion_gb300 import synthetic as syn
+    obs = syn.large_observation(PADDING, subbands=True)
+    sh1, sh2 = dd.getShifts(obs, PADDING), dd.getShiftsStepTwo(obs, PADDING)
+    zapped = syn.zapped_mask(1536, 0.05, 7, PADDING)
+    mapping = syn.identity_mapping(obs, PADDING, subbands=True)
+    inp = syn.make_input(obs, 8, PADDING, seed=3, mode=dd.DD_STEP_ONE, mean=128.0, sigma=20.0)
+    l2 = dd.layout(obs, dd.DD_STEP_TWO, 32, PADDING)
+    dev = f"cuda:{device}"
+    d_in = [torch.from_numpy(inp).to(dev) for _ in range(4)]
+    out = torch.empty(l2.output_bytes // 4, dtype=torch.float32, device=dev)
+    pipe = dd.SubbandPipeline(obs, 8, PADDING, device=device)
+    pipe.setTables(sh1, sh2, zapped, mapping)
+    return obs, sh1, sh2, zapped, mapping, d_in, out, pipe
+
+
+def subband_only(torch, device: int, chunks: int, steps: int, warmup: int):
+    """--subband-only: the pipeline alone with `chunks` time ranges."""
+    obs, _, _, _, _, d_in, out, pipe = subband_inputs(torch, device)
+    pipe.setChunks(chunks)
+    stream = torch.cuda.current_stream()
+    for i in range(warmup):
+        pipe.run(d_in[i % 4], out, stream)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(steps):
+        pipe.run(d_in[i % 4], out, stream)
+    e1.record(stream)
+    pipe.check(stream)
+    ms = e0.elapsed_time(e1) / max(steps, 1)
+    pipe.close()
+    return {"subband_only": True, "chunks": chunks, "steps": steps, "ms_per_batch": ms,
+            "value": obs.getNrDMs(True) * obs.getNrDMs() * obs.getNrSamplesPerBatch() / ms * 1e3,
+            "unit": UNIT}
+
+
 def bench_subband(torch, device: int, steps: int, hbm_peak: float, peak_adds: float):
     """Config 2 in subband mode (1536 ch in 32 subbands, 64 coarse DMs at 6.4
     x 32 fine DMs at 0.2, 24576 samples, uint8 N(128, 20), 5 % zapped): the
@@ -377,6 +420,14 @@ def bench_subband(torch, device: int, steps: int, hbm_peak: float, peak_adds: fl
     t_pipe_ov = timed(lambda i: pipe.run(d_in[i % nbuf], out, stream))
     pipe.check(stream)
     pipe.setOverlap(False)
+    # time-chunked runs (dd_subband_set_chunks): the intermediate is read
+    # back from L2, at the cost of a partial wave per range
+    pipe.setChunks(4)
+    t_chunk = timed(lambda i: pipe.run(d_in[i % nbuf], out, stream))
+    pipe.check(stream)
+    pipe.run(d_in[1], out, stream)
+    out_chunked = out.clone()
+    pipe.setChunks(0)
     t_float = timed(lambda i: (one.run(d_in[i % nbuf], inter, stream),
                                two.run(inter, ref, stream)))
     two.check(stream)
@@ -385,6 +436,10 @@ def bench_subband(torch, device: int, steps: int, hbm_peak: float, peak_adds: fl
     two.run(inter, ref, stream)
     torch.cuda.synchronize()
     exact = bool(torch.equal(out, ref))
+    one.run(d_in[1], inter, stream)
+    two.run(inter, ref, stream)
+    torch.cuda.synchronize()
+    exact_chunked = bool(torch.equal(out_chunked, ref))
     info = pipe.info()
     D1, D2, SB = obs.getNrDMs(True), obs.getNrDMs(), obs.getNrSubbands()
     S, S1 = obs.getNrSamplesPerBatch(), obs.getNrSamplesPerBatch(True)
@@ -398,6 +453,13 @@ def bench_subband(torch, device: int, steps: int, hbm_peak: float, peak_adds: fl
             "serial_value": units / t_pipe, "serial_ms_per_batch": t_pipe * 1e3,
             "float_steps_value": units / t_float, "float_steps_ms": t_float * 1e3,
             "speedup_vs_float_steps": t_float / t_pipe, "bit_exact_vs_float_steps": exact,
+            "chunked": {"chunks": 4, "ms_per_batch": t_chunk * 1e3, "value": units / t_chunk,
+                        "bit_exact_vs_float_steps": exact_chunked,
+                        "what": "dd_subband_set_chunks(4): step two in 4 time ranges, each "
+                                "right after the step-one tiles it reads, so the intermediate "
+                                "is read back from L2 (single-pass ncu: 4.7 MB of DRAM reads "
+                                "per batch instead of 86 MB); slower, as both kernels are "
+                                "bound by instructions and shared memory"},
             "note_speedup": "serial pipeline against the serial float steps",
             "packed": info["packed"], "intermediate_bytes": info["intermediate_bytes"],
             "adds_per_batch": adds, "adds_frac": adds / t_pipe_ov / peak_adds,
@@ -407,7 +469,7 @@ def bench_subband(torch, device: int, steps: int, hbm_peak: float, peak_adds: fl
             "workload": "1536 ch in 32 subbands (5% zapped), 64 coarse DMs at 6.4 x 32 fine "
                         "DMs at 0.2 = 2048 DMs, 24576 samples, uint8 N(128, 20)",
             "note": "hbm_bytes_upper counts the intermediate written and read once through "
-                    "HBM; measured, step two reads all of it from DRAM (L2 hit rate 12%)"}
+                    "HBM; measured (single-pass ncu), step two reads 86 of its 101 MB from DRAM"}
 
 
 def bench_batched(torch, device: int, reps: int = 3, count: int = 40, peak_adds: float = 0.0):
@@ -576,6 +638,9 @@ def main():
     import torch
     import dedispersion_gb300 as dd
     torch.cuda.set_device(local)
+    if args.subband_only is not None:
+        print(json.dumps(subband_only(torch, local, args.subband_only, args.steps, args.warmup)))
+        return
     pg = None
     if world > 1:
         import torch.distributed as tdist

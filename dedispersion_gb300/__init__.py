@@ -369,6 +369,12 @@ class SubbandPipeline:
         finishes (dd_subband_set_overlap): consecutive independent runs only."""
         check(lib().dd_subband_set_overlap(self._h, 1 if enable else 0))
 
+    def setChunks(self, chunks: int) -> None:
+        """Run the two steps interleaved over `chunks` time ranges so that the
+        intermediate is read back from L2 (dd_subband_set_chunks); 0 or 1:
+        each step in one launch."""
+        check(lib().dd_subband_set_chunks(self._h, int(chunks)))
+
     def setPairKernel(self, index: int) -> None:
         check(lib().dd_subband_set_pair_kernel(self._h, int(index)))
 

@@ -116,6 +116,7 @@ SIGNATURES = {
     "dd_subband_info": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_uint64)]),
     "dd_subband_set_pair_kernel": (C.c_int, [_P, C.c_int]),
     "dd_subband_set_overlap": (C.c_int, [_P, C.c_int]),
+    "dd_subband_set_chunks": (C.c_int, [_P, C.c_int]),
     "dd_subband_pair_kernel_count": (C.c_int, []),
     "dd_subband_destroy": (C.c_int, [_P]),
     "dd_subband_dedispersion": (C.c_int, [_OBS, _U32P, _U32P, _P, _F32P, _F32P, _F32P,

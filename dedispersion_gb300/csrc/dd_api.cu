@@ -697,6 +697,32 @@ dd_status plan_launch(const dd_plan *p, const ProblemDesc &P, cudaStream_t strea
   return DD_OK;
 }
 
+// Launches time tiles [base, base + count) of every group and DM tile.
+dd_status plan_launch_range(const dd_plan *p, ProblemDesc P, uint32_t base, uint32_t count,
+                            cudaStream_t stream) {
+  if (base + (uint64_t)count > p->tiles_t)
+    return fail(DD_ERR_INVALID_ARGUMENT, "time tiles %u..%u past %u", base, base + count,
+                p->tiles_t);
+  const uint64_t tiles = (uint64_t)p->nr_groups * p->tiles_d * count;
+  if (tiles == 0) return DD_OK;
+  P.ttile_base = base;
+  P.ttile_count = count;
+  p->kinfo->launch(P, (unsigned)tiles, p->smem, stream);
+  DD_CUDA(cudaGetLastError(), "launch dedispersion kernel");
+  return DD_OK;
+}
+
+// Time tiles, samples per time tile and the largest delay of a built plan.
+dd_status plan_time_tiles(const dd_plan *p, uint32_t *tiles_t, uint32_t *tile_t,
+                          uint32_t *max_delay) {
+  if (dd_status st = ensure_built(p)) return st;
+  if (!p->ready) return fail(DD_ERR_INVALID_ARGUMENT, "plan tables are invalid: %s", p->invalid.c_str());
+  *tiles_t = p->tiles_t;
+  *tile_t = (uint32_t)p->kinfo->tile_t;
+  *max_delay = p->max_delay;
+  return DD_OK;
+}
+
 // The kernel arguments of one run of `p` on the given device buffers; also
 // the rows each group sums (the cost of one of its tiles).
 dd_status plan_problem(const dd_plan *p, const void *d_input, float *d_output,

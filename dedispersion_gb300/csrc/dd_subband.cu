@@ -14,7 +14,10 @@
 // Sums are integers below 2^24 either way, so the output equals the
 // reference's float step one followed by its float step two bit for bit.
 // Otherwise (16-bit or float input, or wider subbands) the pipeline runs the
-// two float steps.
+// two float steps.  With one launch per step most of the intermediate goes
+// through device memory; dd_subband_set_chunks runs the steps interleaved
+// over time ranges so that step two reads it back from L2 (fewer DRAM bytes,
+// more partial waves: slower on compute-bound shapes, hence opt-in).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -31,6 +34,12 @@ void set_last_error(const char *message);
 void plan_set_packed(dd_plan *p, const KernelInfo *k, uint32_t flush_rows);
 void plan_clear_packed(dd_plan *p);
 bool plan_ready(const dd_plan *p);
+dd_status plan_problem(const dd_plan *p, const void *d_input, float *d_output,
+                       ProblemDesc *out, uint64_t *rows_per_group);
+dd_status plan_launch_range(const dd_plan *p, ProblemDesc P, uint32_t base, uint32_t count,
+                            cudaStream_t stream);
+dd_status plan_time_tiles(const dd_plan *p, uint32_t *tiles_t, uint32_t *tile_t,
+                          uint32_t *max_delay);
 
 // Largest step-one sum: live channels of the fullest subband x the largest
 // sample of `bits`-bit input (0 when the width has no integer bound).
@@ -109,6 +118,9 @@ struct dd_subband {
   bool overlap = false;  // step one as a programmatic dependent
   void *inter = nullptr;  // step-one output (packed or float)
   size_t inter_bytes = 0;
+  uint32_t chunks = 0;              // dd_subband_set_chunks (0, 1: whole steps)
+  cudaStream_t side = nullptr;      // step one of a chunked run
+  std::vector<cudaEvent_t> events;  // fork, then one per chunk
   std::vector<float> shifts, shifts2;
   std::vector<uint32_t> zapped, mapping;
 };
@@ -227,12 +239,70 @@ dd_status dd_subband_set_tables(dd_subband *s, const float *shifts, size_t n_shi
   return build(s);
 }
 
+namespace {
+
+// Chunked run: step two's time tiles in `chunks` ranges, each launched right
+// after the step-one tiles it reads (its samples plus the largest step-two
+// delay), so that the intermediate is read back while it is still in L2.
+// Step one runs on a side stream one range ahead of step two: range k + 1's
+// step one writes samples that range k's step two does not read.
+dd_status run_chunked(dd_subband *s, const void *d_input, float *d_output, cudaStream_t stream) {
+  dd::ProblemDesc P1, P2;
+  dd_status st = dd::plan_problem(s->one, d_input, static_cast<float *>(s->inter), &P1, nullptr);
+  if (!st) st = dd::plan_problem(s->two, s->inter, d_output, &P2, nullptr);
+  uint32_t tt1 = 0, T1 = 0, md1 = 0, tt2 = 0, T2 = 0, md2 = 0;
+  if (!st) st = dd::plan_time_tiles(s->one, &tt1, &T1, &md1);
+  if (!st) st = dd::plan_time_tiles(s->two, &tt2, &T2, &md2);
+  if (st) return st;
+  const uint32_t K = std::max<uint32_t>(1, std::min<uint32_t>(s->chunks, tt2));
+  DDS_CUDA(cudaSetDevice(s->device), "select device");
+  if (!s->side)
+    DDS_CUDA(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking), "create stream");
+  while (s->events.size() < K + 1) {
+    cudaEvent_t e = nullptr;
+    DDS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "create event");
+    s->events.push_back(e);
+  }
+  // Step one of this run overwrites the intermediate the previous run's step
+  // two reads: the side stream starts after the caller's stream.
+  DDS_CUDA(cudaEventRecord(s->events[0], stream), "fork");
+  DDS_CUDA(cudaStreamWaitEvent(s->side, s->events[0], 0), "fork");
+  uint32_t done = 0;  // step-one time tiles launched
+  for (uint32_t k = 0; k < K; k++) {
+    const uint32_t a = (uint32_t)((uint64_t)tt2 * k / K), b = (uint32_t)((uint64_t)tt2 * (k + 1) / K);
+    const uint64_t need_samples = (uint64_t)b * T2 + md2 + 1;
+    const uint32_t need = k + 1 == K ? tt1
+                                     : (uint32_t)std::min<uint64_t>(tt1, (need_samples + T1 - 1) / T1);
+    if (need > done) {
+      st = dd::plan_launch_range(s->one, P1, done, need - done, s->side);
+      if (st) return st;
+      done = need;
+    }
+    DDS_CUDA(cudaEventRecord(s->events[1 + k], s->side), "record step one");
+    DDS_CUDA(cudaStreamWaitEvent(stream, s->events[1 + k], 0), "wait step one");
+    st = dd::plan_launch_range(s->two, P2, a, b - a, stream);
+    if (st) return st;
+  }
+  return DD_OK;
+}
+
+}  // namespace
+
 dd_status dd_subband_run(dd_subband *s, const void *d_input, float *d_output, void *stream) {
   if (!s) return fail(DD_ERR_INVALID_ARGUMENT, "pipeline is NULL");
   if (!s->ready) return fail(DD_ERR_INVALID_ARGUMENT, "pipeline has no tables");
+  if (s->chunks > 1) return run_chunked(s, d_input, d_output, static_cast<cudaStream_t>(stream));
   dd_status st = dd_plan_run(s->one, d_input, static_cast<float *>(s->inter), stream);
   if (!st) st = dd_plan_run(s->two, s->inter, d_output, stream);
   return st;
+}
+
+dd_status dd_subband_set_chunks(dd_subband *s, int chunks) {
+  if (!s) return fail(DD_ERR_INVALID_ARGUMENT, "pipeline is NULL");
+  if (chunks < 0 || chunks > 256)
+    return fail(DD_ERR_INVALID_ARGUMENT, "chunks %d out of range (0..256)", chunks);
+  s->chunks = (uint32_t)chunks;
+  return DD_OK;
 }
 
 dd_status dd_subband_check(dd_subband *s, void *stream) {
@@ -276,10 +346,10 @@ int dd_subband_pair_kernel_count(void) {
 dd_status dd_subband_destroy(dd_subband *s) {
   if (!s) return DD_OK;
   drop_plans(s);
-  if (s->inter) {
-    cudaSetDevice(s->device);
-    cudaFree(s->inter);
-  }
+  cudaSetDevice(s->device);
+  if (s->inter) cudaFree(s->inter);
+  for (cudaEvent_t e : s->events) cudaEventDestroy(e);
+  if (s->side) cudaStreamDestroy(s->side);
   delete s;
   return DD_OK;
 }

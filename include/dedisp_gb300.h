@@ -244,6 +244,14 @@ dd_status dd_subband_info(const dd_subband *pipeline, int *packed,
  * after that step two completed.  Only for runs whose input the kernel before
  * them does not write.  Off by default. */
 dd_status dd_subband_set_overlap(dd_subband *pipeline, int enable);
+/* chunks >= 2: each run splits step two's time tiles into `chunks` ranges and
+ * launches each range right after the step-one tiles it reads (its samples
+ * plus the largest step-two delay), step one on a stream of the pipeline's
+ * own one range ahead, so that the intermediate is read back from L2 rather
+ * than from device memory.  0 or 1 (the default): each step over all its
+ * tiles in one launch.  Results are the same bit for bit; the overlap flag
+ * does not apply to chunked runs. */
+dd_status dd_subband_set_chunks(dd_subband *pipeline, int chunks);
 /* Tile configuration of the packed step two (0 .. count - 1; 0 default). */
 dd_status dd_subband_set_pair_kernel(dd_subband *pipeline, int index);
 int dd_subband_pair_kernel_count(void);

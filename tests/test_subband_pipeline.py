@@ -43,11 +43,14 @@ def _oracle_chain(oracle, obs, shifts, shifts2, zapped, inp, mapping, padding, b
     return out
 
 
-def _pipeline(obs, shifts, shifts2, zapped, inp, mapping, padding, bits, pair_kernel=0):
+def _pipeline(obs, shifts, shifts2, zapped, inp, mapping, padding, bits, pair_kernel=0,
+              chunks=0):
     torch = pytest.importorskip("torch")
     p = dd.SubbandPipeline(obs, bits, padding)
     if pair_kernel:
         p.setPairKernel(pair_kernel)
+    if chunks:
+        p.setChunks(chunks)
     p.setTables(shifts, shifts2, zapped, mapping)
     d_in = torch.from_numpy(np.ascontiguousarray(inp).view(np.uint8).reshape(-1)).cuda()
     d_out = torch.zeros(p.layout_out.output_bytes // 4, dtype=torch.float32, device="cuda")
@@ -76,6 +79,23 @@ def test_packed_pipeline_matches_oracle_chain(gpu, oracle, kw):
     want = _oracle_chain(oracle, *args, padding, bits)
     got, info = _pipeline(*args, padding, bits)
     assert info["packed"]
+    np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+@pytest.mark.parametrize("bits,chunks,kw", [
+    (8, 2, dict(D1=7, S=1500)),
+    (8, 5, dict(D1=8, S=2100, D2=20)),
+    (4, 3, dict(D1=6, S=1300)),
+    (8, 200, dict(D1=5, S=1100)),              # more chunks than time tiles
+    (16, 4, dict(D1=5, S=1700)),               # float intermediate
+])
+def test_chunked_pipeline_matches_oracle_chain(gpu, oracle, bits, chunks, kw):
+    """dd_subband_set_chunks: step two in time ranges, each right after the
+    step-one tiles it reads (step one on the pipeline's side stream)."""
+    args = _case(bits=bits, padding=64, seed=13, **kw)
+    want = _oracle_chain(oracle, *args, 64, bits)
+    got, info = _pipeline(*args, 64, bits, chunks=chunks)
+    assert info["packed"] == (bits <= 8)
     np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
 
 
@@ -152,6 +172,14 @@ def test_full_shape_equals_float_steps(gpu):
     one.run(d_in, inter)
     two.run(inter, want)
     two.check()
+    assert torch.equal(got, want)
+    # chunked runs, twice back to back (the second run's step one waits for
+    # the first run's step two)
+    p.setChunks(6)
+    for _ in range(2):
+        got.zero_()
+        p.run(d_in, got)
+    p.check()
     assert torch.equal(got, want)
     for x in (p, one, two):
         x.close()
