@@ -457,8 +457,8 @@ def bench_subband(torch, device: int, steps: int, hbm_peak: float, peak_adds: fl
                         "bit_exact_vs_float_steps": exact_chunked,
                         "what": "dd_subband_set_chunks(4): step two in 4 time ranges, each "
                                 "right after the step-one tiles it reads, so the intermediate "
-                                "is read back from L2 (single-pass ncu: 4.7 MB of DRAM reads "
-                                "per batch instead of 86 MB); slower, as both kernels are "
+                                "is read back from L2 (single-pass ncu: 4.6 MB of DRAM reads "
+                                "per batch instead of 87 MB); slower, as both kernels are "
                                 "bound by instructions and shared memory"},
             "note_speedup": "serial pipeline against the serial float steps",
             "packed": info["packed"], "intermediate_bytes": info["intermediate_bytes"],
@@ -469,7 +469,7 @@ def bench_subband(torch, device: int, steps: int, hbm_peak: float, peak_adds: fl
             "workload": "1536 ch in 32 subbands (5% zapped), 64 coarse DMs at 6.4 x 32 fine "
                         "DMs at 0.2 = 2048 DMs, 24576 samples, uint8 N(128, 20)",
             "note": "hbm_bytes_upper counts the intermediate written and read once through "
-                    "HBM; measured (single-pass ncu), step two reads 86 of its 101 MB from DRAM"}
+                    "HBM; measured (single-pass ncu), step two reads 87 of its 101 MB from DRAM"}
 
 
 def bench_batched(torch, device: int, reps: int = 3, count: int = 40, peak_adds: float = 0.0):
