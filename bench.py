@@ -183,24 +183,82 @@ def read_profile_traffic():
     return int(m.group(1)) if m else None
 
 
-def cpu_sample(obs, shifts, zapped, mapping, inp, target_s, threads):
-    """Time the oracle on a DM prefix sized for ~target_s of wall time;
-    returns (DM-samples/s, dms, seconds)."""
+def cpu_sample(o, sh, z, m, inp, target_s, threads):
+    """Time the oracle port on a DM prefix of the single-step workload sized
+    for ~target_s of wall time; returns (DM-samples/s, dms, seconds).  The
+    prefix keeps the first DM, the DM step and the full dispersed length, so
+    every delay is the full workload's.  ``o`` is the observation struct
+    (oracle.types or the engine's, same layout)."""
     import oracle
-    out = np.zeros(obs.getNrDMs() * dd_out_row(obs), dtype=np.float32)
+    out = np.zeros(o.nr_dms * out_row(o), dtype=np.float32)
     dms = 2
     while True:
         t = time.perf_counter()
-        oracle.dedispersion(obs.c, zapped, mapping, inp, out, shifts, PADDING, 8, 0, dms, threads)
+        oracle.dedispersion(o, z, m, inp, out, sh, PADDING, 8, 0, dms, threads)
         dt = time.perf_counter() - t
-        if dt >= target_s * 0.5 or dms >= obs.getNrDMs():
-            return dms * obs.getNrSamplesPerBatch() / dt, dms, dt
-        dms = min(obs.getNrDMs(), max(dms + 1, int(dms * target_s / max(dt, 1e-3))))
+        if dt >= target_s * 0.5 or dms >= o.nr_dms:
+            return dms * o.nr_samples_per_batch / dt, dms, dt
+        dms = min(o.nr_dms, max(dms + 1, int(dms * target_s / max(dt, 1e-3))))
 
 
-def dd_out_row(obs):
-    import dedispersion_gb300 as dd
-    return dd.pad(obs.getNrSamplesPerBatch(), PADDING // 4)
+def reference_cpu_sample(o, sh, z, m, inp, target_s):
+    """The reference's own CPU template (include/Dedispersion.hpp:70-109,
+    compiled unmodified into oracle/_ref/libddref.so), single-threaded as the
+    reference runs it, on a DM prefix sized for ~target_s.  None where that
+    library was not built (the reference's sources are not on this machine).
+    Returns (DM-samples/s, dms, seconds)."""
+    import ctypes as C
+    import oracle
+    if not oracle.REF_LIB.exists():
+        return None
+    ref = oracle.reference()
+    U32P, F32P = C.POINTER(C.c_uint32), C.POINTER(C.c_float)
+    dms = 1
+    while True:
+        sub = type(o).from_buffer_copy(o)
+        sub.nr_dms = dms          # same first DM, step and dispersed length
+        out = np.zeros(dms * out_row(o), dtype=np.float32)
+        t = time.perf_counter()
+        rc = ref.ddref_dedispersion(C.byref(sub), z.ctypes.data_as(U32P), z.size,
+                                    m.ctypes.data_as(U32P), m.size,
+                                    C.c_void_p(inp.ctypes.data), inp.size,
+                                    out.ctypes.data_as(F32P), out.size,
+                                    sh.ctypes.data_as(F32P), sh.size, PADDING, 8)
+        dt = time.perf_counter() - t
+        if rc != 0:
+            return None
+        if dt >= target_s * 0.5 or dms >= o.nr_dms:
+            return dms * o.nr_samples_per_batch / dt, dms, dt
+        dms = min(o.nr_dms, max(dms + 1, int(dms * target_s / max(dt, 1e-3))))
+
+
+def cpu_baseline(o, sh, z, m, inp, target_s):
+    """cpu_baseline object: the oracle port on every host thread (the figure),
+    the same port on one thread, and the reference's own code on one thread
+    where it was built here."""
+    threads = os.cpu_count() or 1
+    val, dms, dt = cpu_sample(o, sh, z, m, inp, target_s, threads)
+    one, dms1, dt1 = cpu_sample(o, sh, z, m, inp, target_s / 2, 1)
+    line = {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"DMs 0..{dms - 1} of 2048 (all 24576 samples, 1536 channels), "
+                      f"{dt:.2f} s wall on {threads} threads",
+            "single_thread": {"value": one, "cores": 1, "kind": "port",
+                              "sample": f"DMs 0..{dms1 - 1}, {dt1:.2f} s on 1 thread"}}
+    ref = reference_cpu_sample(o, sh, z, m, inp, target_s / 2)
+    if ref is None:
+        line["reference_code"] = ("not run: the reference's sources are not on this machine, "
+                                  "so oracle/_ref was not built; the port is bit-identical to it "
+                                  "(tests/test_oracle.py)")
+    else:
+        line["reference_code"] = {"value": ref[0], "cores": 1, "kind": "reference",
+                                  "sample": f"DMs 0..{ref[1] - 1}, {ref[2]:.2f} s on 1 thread"}
+    return line
+
+
+def out_row(o):
+    """Padded output row of the single-step layout, in floats."""
+    q = PADDING // 4
+    return -(-o.nr_samples_per_batch // q) * q
 
 
 def bench_detect(torch, plan, d_in, d_out, stream, D, S, steps):
@@ -544,21 +602,35 @@ def bench_batched(torch, device: int, reps: int = 3, count: int = 40, peak_adds:
                         "0.1-0.5, 2/4/8-bit uniform input, 5% zapped"}
 
 
+def served_adds(server):
+    """Algorithmic adds of one batch of every admitted beam: live channels x
+    DMs x samples for a single-step beam; step one (live channels x coarse
+    DMs x step-one samples) plus step two (subbands x DMs x samples) for a
+    subband beam."""
+    import dedispersion_gb300 as dd
+    total = 0
+    for st in server.streams:
+        cfg = st.cfg
+        live = int((st.zapped[:cfg.channels] == 0).sum())
+        if cfg.subband:
+            d1 = cfg.dms // cfg.dms_per_subband_dm
+            tail2 = dd.layout(st.obs, dd.DD_STEP_TWO, 32, cfg.padding, st.shifts2).max_delay
+            total += live * d1 * (cfg.samples + tail2) + cfg.subbands * cfg.dms * cfg.samples
+        else:
+            total += live * cfg.dms * cfg.samples
+    return total
+
+
 def bench_served(device: int, batches: int = 6, compression: float = 16.0,
-                 double_buffer: bool = True):
+                 double_buffer: bool = True, runs: int = 3, peak_adds: float = 0.0):
     """12 beams streaming 2.048 s batches (1536 ch, 25000 samples at 81.92 us,
     8-bit), DM ranges of 1024-4096 DMs at step 0.2, alternating single-step and
-    subband (32 subbands) modes, admitted against a 150 GB budget.  Two runs:
-    Poisson-jittered arrivals on a clock 16x faster than real time (latency),
-    and all batches at once (throughput)."""
+    subband (32 subbands) modes, admitted against a 150 GB budget.  After a
+    warm-up that pushes every staging buffer of every beam once, `runs` runs
+    of each: Poisson-jittered arrivals on a clock 16x faster than real time
+    (latency), and all batches at once (throughput); medians and spreads."""
     from dedispersion_gb300 import serving
-    rng = np.random.default_rng(77)
-    cfgs = []
-    for b in range(12):
-        dms = int(rng.integers(8, 33)) * 128
-        cfgs.append(serving.BeamConfig(name=f"beam{b}", dms=dms, subband=(b % 2 == 1),
-                                       seed=100 + b, padding=PADDING,
-                                       double_buffer=double_buffer))
+    cfgs = serving.served_beams(12, seed=77, padding=PADDING, double_buffer=double_buffer)
     server = serving.Server(budget_bytes=150 * 10**9, device=device)
     for c in cfgs:
         server.admit(c)
@@ -572,47 +644,69 @@ def bench_served(device: int, batches: int = 6, compression: float = 16.0,
         np.copyto(staging[:, :cfgs[b].samples], data[b][k % 2])
 
     period = cfgs[0].period
-    # warm-up: one batch per beam
-    server.serve([(0.0, b, 0) for b in range(len(cfgs))], source)
-    sched = serving.poisson_schedule(len(cfgs), batches, period, 0.1 * period, seed=9)
-    timed = server.serve(sched, source, time_compression=compression, deadline=period)
-    burst = server.serve([(0.0, b, k) for k in range(batches) for b in range(len(cfgs))], source,
-                         deadline=period)
-    lat, thr = timed.summary(), burst.summary()
-    out = {"value": thr["throughput_dm_samples_per_s"], "unit": UNIT,
-           "p50_latency_s": lat["p50_latency_s"], "p99_latency_s": lat["p99_latency_s"],
-           "max_latency_s": lat["max_latency_s"], "deadline_s": period,
-           "deadline_misses": lat["deadline_misses"], "batches": lat["batches"],
+    nbuf = max(s.nbuf for s in server.streams)
+    # warm-up: every staging buffer (and so every recorded graph) of every beam
+    server.serve([(0.0, b, k) for k in range(nbuf) for b in range(len(cfgs))], source)
+    lat_runs, thr_runs = [], []
+    for r in range(runs):
+        sched = serving.poisson_schedule(len(cfgs), batches, period, 0.1 * period, seed=9 + r)
+        lat_runs.append(server.serve(sched, source, time_compression=compression,
+                                     deadline=period).summary())
+        thr_runs.append(server.serve([(0.0, b, k) for k in range(batches)
+                                      for b in range(len(cfgs))], source,
+                                     deadline=period).summary())
+    med = lambda xs: float(statistics.median(xs))  # noqa: E731
+    thr = [t["throughput_dm_samples_per_s"] for t in thr_runs]
+    p50 = [t["p50_latency_s"] for t in lat_runs]
+    p99 = [t["p99_latency_s"] for t in lat_runs]
+    units_per_round = sum(st.dm_samples for st in server.streams)
+    adds_per_round = served_adds(server)
+    value = med(thr)
+    out = {"value": value, "unit": UNIT, "runs": runs,
+           "value_spread": [min(thr), max(thr)],
+           "p50_latency_s": med(p50), "p50_spread_s": [min(p50), max(p50)],
+           "p99_latency_s": med(p99), "p99_spread_s": [min(p99), max(p99)],
+           "max_latency_s": max(t["max_latency_s"] for t in lat_runs), "deadline_s": period,
+           "deadline_misses": sum(t["deadline_misses"] for t in lat_runs),
+           "batches_per_run": lat_runs[0]["batches"],
            "time_compression": compression,
-           "offered_load_throughput": lat["throughput_dm_samples_per_s"],
+           "offered_load_throughput": med([t["throughput_dm_samples_per_s"] for t in lat_runs]),
            "beams": len(cfgs), "subband_beams": sum(c.subband for c in cfgs),
+           "adds_per_round": adds_per_round,
+           "adds_frac": (value / units_per_round * adds_per_round / peak_adds
+                         if peak_adds else None),
            "admitted_device_bytes": server.used, "budget_bytes": server.budget,
            "double_buffered": double_buffer,
            "workload": "12 beams x 25000-sample 8-bit batches, 1536 ch, 1024-4096 DMs at 0.2, "
                        "single-step and 32-subband streams, tail carried on the device; value = "
-                       "all batches queued at once, latency = Poisson-jittered arrivals at 16x "
-                       "real time, host-in to host-out"}
+                       "median over runs of all batches queued at once, latency = "
+                       "Poisson-jittered arrivals at 16x real time, host-in to host-out"}
     server.close()
     return out
 
 
 def run_reference(args, rank, world):
+    """The CPU arm: the oracle port (a loop-for-loop port of the reference's
+    dedispersion, bit-identical to it) on every host thread, each step a DM
+    prefix of the workload.  Built from numpy and the oracle alone: the
+    engine's library is never loaded in this process."""
     if rank != 0:
         return
-    obs, shifts, zapped, mapping, inp = workload()
+    from oracle import workload as owl
+    o, sh, z, m, inp = owl.single_step(seed=beam_seed(0), padding=PADDING)
     threads = os.cpu_count() or 1
     import oracle
-    out = np.zeros(obs.getNrDMs() * dd_out_row(obs), dtype=np.float32)
+    out = np.zeros(o.nr_dms * out_row(o), dtype=np.float32)
     # size one step's DM prefix for ~1/(steps+warmup) of a ~60 s budget
-    _, dms, dt = cpu_sample(obs, shifts, zapped, mapping, inp,
-                            max(0.5, 60.0 / (args.steps + args.warmup)), threads)
+    _, dms, dt = cpu_sample(o, sh, z, m, inp, max(0.5, 60.0 / (args.steps + args.warmup)),
+                            threads)
     for _ in range(args.warmup):
-        oracle.dedispersion(obs.c, zapped, mapping, inp, out, shifts, PADDING, 8, 0, dms, threads)
+        oracle.dedispersion(o, z, m, inp, out, sh, PADDING, 8, 0, dms, threads)
     t = time.perf_counter()
     for _ in range(args.steps):
-        oracle.dedispersion(obs.c, zapped, mapping, inp, out, shifts, PADDING, 8, 0, dms, threads)
+        oracle.dedispersion(o, z, m, inp, out, sh, PADDING, 8, 0, dms, threads)
     elapsed = time.perf_counter() - t
-    value = args.steps * dms * obs.getNrSamplesPerBatch() / elapsed
+    value = args.steps * dms * o.nr_samples_per_batch / elapsed
     sample = (f"DMs 0..{dms - 1} of 2048 x 24576 samples x 1536 channels per step "
               f"(same delays as the full workload)")
     print(json.dumps({
@@ -623,6 +717,8 @@ def run_reference(args, rank, world):
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's own CPU code needs its sources, which are not on the GPU "
+                "machine; the port timed here equals it bit for bit (tests/test_oracle.py)",
     }), flush=True)
 
 
@@ -729,7 +825,13 @@ def main():
     e2e_value = job_value(world, e2e_steps, D, S, t_e2e)
 
     sm_mhz = clocks.get("sm_mhz") or 2070.0
-    peak_adds = SMS * LANES * sm_mhz * 1e6
+    formula_adds = SMS * LANES * sm_mhz * 1e6
+    # The add roofline's denominator, measured on this GPU now: the faster of
+    # a float-add and an integer-add stream over every SM (dd_measure_add_rate).
+    with ClockSampler(local) as peak_clk:
+        rates = dd.measure_add_rate(local, 3)
+    peak_clocks = peak_clk.summary()
+    peak_adds = max(rates["fadd_per_s"], rates["iadd_per_s"])
     hbm_peak = 6784.2
     try:
         hbm_peak = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"]
@@ -739,7 +841,7 @@ def main():
     # The served line runs before the lines that leave large host arrays and
     # many plans behind: its latencies are host-driven.
     gc.collect()
-    served = bench_served(local) if not args.no_served else None
+    served = bench_served(local, peak_adds=peak_adds) if not args.no_served else None
     ingest_line = bench_ingest(torch, inp, lay, obs, stream)
     subband = bench_subband(torch, local, max(10, min(args.steps, 50)), hbm_peak, peak_adds)
     float32 = bench_float(torch, local, max(3, min(args.steps, 10)), peak_adds)
@@ -755,9 +857,7 @@ def main():
     executed_adds = plan.adds()
     kernel_name = next((k.name for k in dd.kernels()
                         if k.conf.print() == plan.conf().print()), plan.conf().print())
-    cpu_threads = os.cpu_count() or 1
-    cpu_val, cpu_dms, cpu_dt = cpu_sample(obs, shifts, zapped, mapping, inp, args.cpu_seconds,
-                                          cpu_threads)
+    cpu_line = cpu_baseline(obs.c, shifts, zapped, mapping, inp, args.cpu_seconds)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3,
@@ -774,8 +874,16 @@ def main():
         "roofline": {"bound": "alu", "achieved": achieved_adds / 1e9, "peak": peak_adds / 1e9,
                      "unit": "Gadd/s", "frac": achieved_adds / peak_adds,
                      "traffic": traffic,
-                     "peak_source": f"scalar add issue rate: {SMS} SMs x {LANES} lanes x "
-                                    f"{sm_mhz:.0f} MHz (median SM clock sampled during the run)",
+                     "peak_source": "measured: the faster of a float-add and a 32-bit "
+                                    "integer-add stream over every SM, timed with CUDA events "
+                                    "in this run (dd_measure_add_rate)",
+                     "peak_measured": {"fadd_per_s": rates["fadd_per_s"],
+                                       "iadd_per_s": rates["iadd_per_s"],
+                                       "sm_mhz": peak_clocks.get("sm_mhz"),
+                                       "reasons": peak_clocks.get("reasons")},
+                     "peak_formula": {"adds_per_s": formula_adds,
+                                      "what": f"{SMS} SMs x {LANES} lanes x {sm_mhz:.0f} MHz "
+                                              "(median SM clock of the timed region)"},
                      "adds_per_launch": adds_per_launch,
                      "kernel": kernel_name,
                      "executed": {
@@ -789,9 +897,7 @@ def main():
                              "peak_gbs": hbm_peak,
                              "frac": compulsory / per_launch_s / 1e9 / hbm_peak,
                              "compulsory_bytes_per_launch": compulsory}},
-        "cpu_baseline": {"value": cpu_val, "unit": UNIT, "cores": cpu_threads, "kind": "port",
-                         "sample": f"DMs 0..{cpu_dms - 1} of 2048 (all 24576 samples, 1536 "
-                                   f"channels), {cpu_dt:.2f} s wall on {cpu_threads} threads"},
+        "cpu_baseline": cpu_line,
         "clocks": clocks,
         "gpu_launches": args.steps * plan.launches(),
         "serial_launches": {"ms_per_step": t_serial / args.steps * 1e3,

@@ -41,6 +41,14 @@ def pad(value: int, padding: int) -> int:
     return int(lib().dd_pad(int(value), int(padding)))
 
 
+def measure_add_rate(device: int = 0, repeats: int = 3) -> dict:
+    """Measured float and 32-bit integer add throughput of a GPU, adds/s
+    (dd_measure_add_rate): the denominator of the add roofline."""
+    f, i = C.c_double(0), C.c_double(0)
+    check(lib().dd_measure_add_rate(device, repeats, C.byref(f), C.byref(i)))
+    return {"fadd_per_s": f.value, "iadd_per_s": i.value}
+
+
 def device_count() -> int:
     n = C.c_int(0)
     check(lib().dd_device_count(C.byref(n)))
@@ -604,6 +612,12 @@ class Plan:
         """Launch runs as programmatic dependents of the stream's previous
         kernel (dd_plan_set_overlap): only for consecutive independent runs."""
         check(lib().dd_plan_set_overlap(self._h, 1 if enable else 0))
+
+    def setWaitLimit(self, ns: int) -> None:
+        """Limit of each device-side wait for a staged copy, in ns (0: the
+        default 2 s); a run whose wait runs out makes check() raise with
+        DD_ERR_TIMEOUT (dd_plan_set_wait_limit)."""
+        check(lib().dd_plan_set_wait_limit(self._h, int(ns)))
 
     def adds(self) -> int:
         """Integer adds one run performs (tile padding included)."""

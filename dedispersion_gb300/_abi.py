@@ -138,6 +138,7 @@ SIGNATURES = {
     "dd_plan_get_conf": (C.c_int, [_P, _CONF]),
     "dd_plan_adds": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "dd_plan_set_overlap": (C.c_int, [_P, C.c_int]),
+    "dd_plan_set_wait_limit": (C.c_int, [_P, C.c_uint32]),
     "dd_filterbank_info_read": (C.c_int, [C.c_char_p, _P]),
     "dd_filterbank_read": (C.c_int, [C.c_char_p, _P, C.c_uint64, C.c_uint64, _P]),
     "dd_filterbank_observation": (C.c_int, [_P, _P]),
@@ -182,6 +183,8 @@ SIGNATURES = {
     "dd_mlp_train": (C.c_int, [_P, _F32P, _F32P, C.c_uint32, C.c_uint32, C.c_float, _F32P]),
     "dd_mlp_destroy": (C.c_int, [_P]),
     "dd_plan_time": (C.c_int, [_P, _P, _P, C.c_uint32, C.c_uint32, _F32P, _F32P]),
+    "dd_measure_add_rate": (C.c_int, [C.c_int, C.c_uint32, C.POINTER(C.c_double),
+                                      C.POINTER(C.c_double)]),
 }
 
 _lib: C.CDLL | None = None

@@ -69,18 +69,5 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     return LIB
 
 
-def build_oracle(verbose: bool = False) -> None:
-    """Builds the CPU oracle (test infrastructure) and, where the reference's
-    sources are present, the reference's own CPU code beside it."""
-    oracle = PKG.parent / "oracle"
-    _run(["make", "-s", "-C", str(oracle), "all"])
-    ref = Path(os.environ.get("DD_REFERENCE", "/root/reference"))
-    if (ref / "include" / "Dedispersion.hpp").exists():
-        _run(["make", "-s", "-C", str(oracle), "ref", f"REFERENCE={ref}"])
-    if verbose:
-        print("built oracle")
-
-
 if __name__ == "__main__":
     build(verbose=True, force="--force" in sys.argv)
-    build_oracle(verbose=True)

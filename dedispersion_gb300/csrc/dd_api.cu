@@ -300,6 +300,12 @@ struct dd_plan {
   uint32_t flush_rows = 0;  // step two: rows per 16-bit lane flush
   uint32_t max_delay = 0;   // largest row delay of the built tables
   bool overlap = false;     // dd_plan_set_overlap
+  // A kernel reading the device tables was enqueued since they were last
+  // uploaded: the next upload first waits for the device (the run may still
+  // be in flight on a non-blocking stream, which the synchronous upload
+  // copies do not order against).
+  mutable bool launched = false;
+  uint32_t wait_ns = 0;     // dd_plan_set_wait_limit (0: the kernels' default)
 };
 
 namespace {
@@ -494,6 +500,10 @@ dd_status rebuild(dd_plan *p) {
   }
   // Upload.
   DeviceGuard g(p->device);
+  if (p->launched) {
+    DD_CUDA(cudaDeviceSynchronize(), "wait for runs reading the old tables");
+    p->launched = false;
+  }
   if (p->groups.size() > p->cap_groups) {
     if (p->d_groups) cudaFree(p->d_groups);
     p->d_groups = nullptr;
@@ -692,6 +702,7 @@ int plan_family(const dd_plan *p) {
 dd_status plan_launch(const dd_plan *p, const ProblemDesc &P, cudaStream_t stream) {
   const uint64_t tiles = (uint64_t)p->nr_groups * p->tiles_d * p->tiles_t;
   if (tiles == 0) return DD_OK;
+  p->launched = true;
   p->kinfo->launch(P, (unsigned)tiles, p->smem, stream);
   DD_CUDA(cudaGetLastError(), "launch dedispersion kernel");
   return DD_OK;
@@ -707,6 +718,7 @@ dd_status plan_launch_range(const dd_plan *p, ProblemDesc P, uint32_t base, uint
   if (tiles == 0) return DD_OK;
   P.ttile_base = base;
   P.ttile_count = count;
+  p->launched = true;
   p->kinfo->launch(P, (unsigned)tiles, p->smem, stream);
   DD_CUDA(cudaGetLastError(), "launch dedispersion kernel");
   return DD_OK;
@@ -757,6 +769,7 @@ dd_status plan_problem(const dd_plan *p, const void *d_input, float *d_output,
   P.tma = (d.row_bytes % 16 == 0 && reinterpret_cast<uintptr_t>(d_input) % 16 == 0) ? 1u : 0u;
   P.out_vec4 = (d.out_row % 4 == 0 && reinterpret_cast<uintptr_t>(d_output) % 16 == 0) ? 1u : 0u;
   P.mul_hi8 = 1u << 24;
+  P.wait_ns = p->wait_ns;
   if (p->use_delay_tables) {
     P.delay_rows = (uint32_t)p->delay_shift.size();
     P.delay_rel = p->d_delay_rel;
@@ -1080,6 +1093,7 @@ dd_status dd_plan_run(dd_plan *p, const void *d_input, float *d_output, void *st
   if (tiles == 0) return DD_OK;
   DeviceGuard g(p->device);
   if (!g.ok) return fail(DD_ERR_CUDA, "cannot select device %d", p->device);
+  p->launched = true;
   // The shared, swar8 and pair tiles take part (the scalar tile launches as
   // usual).
   if (p->overlap && p->kinfo->family != dd::kFamilyScalar) {
@@ -1102,6 +1116,12 @@ dd_status dd_plan_run(dd_plan *p, const void *d_input, float *d_output, void *st
   }
   p->kinfo->launch(P, (unsigned)tiles, p->smem, static_cast<cudaStream_t>(stream));
   DD_CUDA(cudaGetLastError(), "launch dedispersion kernel");
+  return DD_OK;
+}
+
+dd_status dd_plan_set_wait_limit(dd_plan *p, uint32_t ns) {
+  if (!p) return fail(DD_ERR_INVALID_ARGUMENT, "plan is NULL");
+  p->wait_ns = ns;
   return DD_OK;
 }
 
@@ -1129,6 +1149,7 @@ dd_status dd_plan_run_stats(dd_plan *p, const void *d_input, float *d_output,
   if (tiles == 0) return DD_OK;
   const bool fused = p->kinfo->family == dd::kFamilyShared8;
   if (fused) P.accum = reinterpret_cast<unsigned long long *>(d_accum);
+  p->launched = true;
   p->kinfo->launch(P, (unsigned)tiles, p->smem, s);
   DD_CUDA(cudaGetLastError(), "launch dedispersion kernel");
   if (!fused)

@@ -145,9 +145,31 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
-// Bounded wait for the phase with `parity` to complete.
+// The bounded wait's limit of a problem (ProblemDesc::wait_ns, else 2 s).
+__device__ __forceinline__ unsigned long long wait_limit(const ProblemDesc &P) {
+  return P.wait_ns ? (unsigned long long)P.wait_ns : kWaitNs;
+}
+
+// Non-blocking test of the phase with `parity`.
+__device__ __forceinline__ bool mbar_test_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for the phase with `parity` to complete.  A limit below a
+// microsecond is one non-blocking test (try_wait may itself suspend for
+// about that long), so that such a limit reliably runs out on a copy that
+// has not landed yet.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
                                           unsigned long long limit_ns) {
+  if (limit_ns < 1000ull) return mbar_test_wait(bar, parity);
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long start = global_ns();
   for (;;) {
@@ -434,7 +456,7 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
   for (uint32_t s = 0; s < nst; ++s) {
     const uint32_t gs = sc + s, slot = gs % kNRaw, area = gs & 1u;
     const uint32_t cnt = (K - s * CH) < (uint32_t)CH ? (K - s * CH) : CH;
-    const bool ok = mbar_wait(S.bars + slot, (gs / kNRaw) & 1u, kWaitNs);
+    const bool ok = mbar_wait(S.bars + slot, (gs / kNRaw) & 1u, wait_limit(P));
     if (!P.tma) {
       copy_stage_plain<CH, TY>(P, G, S, s, slot, cnt);
       __syncthreads();
@@ -679,7 +701,7 @@ __device__ __forceinline__ bool scalar_tile(const ProblemDesc &P,
   for (uint32_t s = 0; s < nst; ++s) {
     const uint32_t gs = sc + s, slot = gs % kNRaw, area = gs & 1u;
     const uint32_t cnt = (K - s * CH) < (uint32_t)CH ? (K - s * CH) : CH;
-    const bool ok = mbar_wait(S.bars + slot, (gs / kNRaw) & 1u, kWaitNs);
+    const bool ok = mbar_wait(S.bars + slot, (gs / kNRaw) & 1u, wait_limit(P));
     if (!P.tma) {
       copy_stage_plain<CH, TY>(P, G, S, s, slot, cnt);
       __syncthreads();
@@ -795,7 +817,7 @@ __device__ __forceinline__ bool pair_tile(const ProblemDesc &P, uint32_t g,
   for (uint32_t s = 0; s < nst; ++s) {
     const uint32_t gs = sc + s, slot = gs % kNRaw, area = gs & 1u;
     const uint32_t cnt = (K - s * CH) < (uint32_t)CH ? (K - s * CH) : CH;
-    const bool ok = mbar_wait(S.bars + slot, (gs / kNRaw) & 1u, kWaitNs);
+    const bool ok = mbar_wait(S.bars + slot, (gs / kNRaw) & 1u, wait_limit(P));
     if (!P.tma) {
       copy_stage_plain<CH, TY>(P, G, S, s, slot, cnt);
       __syncthreads();

@@ -128,6 +128,11 @@ struct ProblemDesc {
   uint32_t pair_d1;       // coarse DMs
   uint32_t flush_rows;    // rows summed in 16-bit lanes before widening
   uint64_t pair_stride;   // floats from a coarse DM 2p row to its 2p + 1 row
+  // Limit of each bounded wait for a staged copy, in ns (0: the default of
+  // 2 s).  A tiny limit makes the waits run out: the test of the timeout
+  // path sets it (dd_plan_set_wait_limit).  The drain after a timeout keeps
+  // its own limit, so every copy in flight lands before a CTA exits.
+  uint32_t wait_ns;
 };
 
 // One entry of the kernel registry: a compiled tile configuration.

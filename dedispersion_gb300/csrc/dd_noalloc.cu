@@ -16,7 +16,9 @@
 // rejected with DD_ERR_UNSUPPORTED.  Every call shares the one array and it
 // keeps the last call's contents, so calls that overlap on the GPU (two host
 // threads, or two streams) race; host threads are serialized by a mutex here,
-// but work queued on different streams by other means is not.
+// but work queued on different streams by other means is not.  Each call
+// waits on its stream for its own kernel (it reads the status word back)
+// before it returns; the stream must belong to the current device.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -125,9 +127,21 @@ extern "C" dd_status dd_dedispersion_noalloc(const dd_observation *o, const uint
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(e, "current device");
   if (dev < 0 || dev >= kMaxDevices) return fail(DD_ERR_UNSUPPORTED, "device %d", dev);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (s != nullptr) {
+    // The scratch address and the kernel launch are the current device's:
+    // a stream of another device would be handed a foreign address.
+    int sdev = -1;
+    e = cudaStreamGetDevice(s, &sdev);
+    if (e != cudaSuccess) return cuda_fail(e, "device of the stream");
+    if (sdev != dev)
+      return fail(DD_ERR_INVALID_ARGUMENT,
+                  "the stream belongs to device %d but device %d is current", sdev, dev);
+  }
   if (!g_scratch_addr[dev]) {
-    // Set-up, once per device, with that device current.  Do the first call
-    // on a device before capturing any stream into a graph.
+    // Set-up, once per device, with that device current: the first call on
+    // a device does it, so that first call should come before any stream
+    // capture begins.
     void *addr = nullptr;
     e = cudaGetSymbolAddress(&addr, dd_noalloc_scratch);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(dd_noalloc_scratch)");
@@ -186,7 +200,6 @@ extern "C" dd_status dd_dedispersion_noalloc(const dd_observation *o, const uint
   e = cudaFuncSetAttribute(k->func, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
   if (e != cudaSuccess) return cuda_fail(e, "set kernel shared memory");
 
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
   // The status word must start at zero; the tables are overwritten in full.
   e = cudaMemsetAsync(scratch, 0, sizeof(uint32_t), s);
   if (e == cudaSuccess)

@@ -243,7 +243,7 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
 
   for (uint32_t s = 0; s < nst; ++s) {
     const uint32_t gs = sc + s, slot = gs % kSharedSlots;
-    const bool ok = mbar_wait(bars + slot, (gs / kSharedSlots) & 1u, kWaitNs);
+    const bool ok = mbar_wait(bars + slot, (gs / kSharedSlots) & 1u, wait_limit(P));
     const uint16_t *tb =
         reinterpret_cast<const uint16_t *>(smem + L.off_table + slot * P.table_bytes);
     uint8_t *rs = smem + L.off_raw + slot * kStageRows * L.raw_bytes;

@@ -218,8 +218,12 @@ dd_status record(dd_stream *s) {
     cudaError_t e = cudaStreamEndCapture(s->capture, &s->graph[b]);
     if (st) return st;
     if (e == cudaSuccess) e = cudaGraphInstantiate(&s->exec[b], s->graph[b], 0);
+    // Upload now, so that the first push of each buffer does not pay for it
+    // inside a served batch's latency.
+    if (e == cudaSuccess) e = cudaGraphUpload(s->exec[b], s->capture);
     if (e != cudaSuccess) return cuda_fail(e, "record stream graph");
   }
+  DDS_CUDA(cudaStreamSynchronize(s->capture), "upload stream graphs");
   return DD_OK;
 }
 

@@ -185,6 +185,21 @@ class Stream:
             pass
 
 
+def served_beams(count: int = 12, seed: int = 77, padding: int = 128,
+                 double_buffer: bool = True) -> list[BeamConfig]:
+    """The 12-beam real-time workload: 2.048 s batches (1536 channels, 25000
+    samples at 81.92 us, 8-bit), each beam's DM count drawn uniformly from
+    1024-4096 in steps of 128 at step 0.2, even beams single step and odd
+    beams 32-subband, 5 % of channels zapped from the beam's seed."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for b in range(count):
+        dms = int(rng.integers(8, 33)) * 128
+        out.append(BeamConfig(name=f"beam{b}", dms=dms, subband=(b % 2 == 1), seed=100 + b,
+                              padding=padding, double_buffer=double_buffer))
+    return out
+
+
 def poisson_schedule(beams: int, batches: int, period: float, jitter: float, seed: int):
     """Arrivals (time, beam, batch): batch k of beam b at phase_b + k * period +
     Exp(jitter), sorted by time."""
@@ -198,9 +213,32 @@ def poisson_schedule(beams: int, batches: int, period: float, jitter: float, see
     return out
 
 
+# Marks a scheduled batch whose data never arrived (see Server.serve).
+DROPPED = "dropped"
+
+
+def inject(schedule, late: dict | None = None, dropped=()):
+    """A copy of `schedule` [(arrival s, beam, batch)] with faults injected on
+    the host: ``late`` maps (beam, batch) to a delay in seconds added to that
+    batch's arrival; ``dropped`` lists (beam, batch) pairs whose data never
+    arrive.  Entries become (nominal arrival, beam, batch, delay or DROPPED)."""
+    late = late or {}
+    dropped = set(dropped)
+    out = []
+    for t, b, k in (e[:3] for e in schedule):
+        if (b, k) in dropped:
+            out.append((t, b, k, DROPPED))
+        else:
+            out.append((t, b, k, float(late.get((b, k), 0.0))))
+    return out
+
+
 @dataclass
 class ServeReport:
-    latencies: list = field(default_factory=list)  # seconds, per batch
+    latencies: list = field(default_factory=list)  # seconds, per delivered batch
+    misses: list = field(default_factory=list)     # (beam, batch) past their deadline
+    dropped: list = field(default_factory=list)    # (beam, batch) whose data never came
+    late: list = field(default_factory=list)       # (beam, batch) that arrived late
     dm_samples: int = 0
     wall: float = 0.0
     deadline: float = 0.0
@@ -213,7 +251,9 @@ class ServeReport:
                 "p99_latency_s": float(np.percentile(lat, 99)),
                 "max_latency_s": float(lat.max()),
                 "deadline_s": self.deadline,
-                "deadline_misses": int((lat > self.deadline).sum()),
+                "deadline_misses": len(self.misses),
+                "dropped_batches": len(self.dropped),
+                "late_batches": len(self.late),
                 "throughput_dm_samples_per_s": self.dm_samples / self.wall if self.wall else 0.0,
                 "wall_s": self.wall, "time_compression": self.time_compression}
 
@@ -248,15 +288,37 @@ class Server:
 
     def serve(self, schedule, source, consumer=None, time_compression: float = 1.0,
               deadline: float | None = None) -> ServeReport:
-        """Run `schedule` [(arrival s, beam, batch)].  source(beam, batch,
-        staging) fills a beam's pinned staging input; consumer(beam, batch,
-        output) sees each finished output (pinned host rows)."""
+        """Run `schedule`: entries (arrival s, beam, batch), or (nominal
+        arrival s, beam, batch, delay s or DROPPED) as :func:`inject` makes
+        them.  source(beam, batch, staging) fills a beam's pinned staging
+        input; consumer(beam, batch, output) sees each finished output
+        (pinned host rows).
+
+        A beam's batches are pushed in batch order, whatever order they
+        arrive in: the device ring carries each batch's tail into the next.
+        A late batch (delay > 0) arrives `delay` after its nominal time; its
+        later batches wait for it.  A dropped batch is pushed as zeros, so
+        that the ring stays aligned in time, and is neither delivered nor
+        timed.  Latency runs from a batch's actual arrival to its output on
+        the host; a batch misses its deadline when its output lands more
+        than `deadline` (default: the longest batch period) after its
+        nominal arrival."""
         import torch
         n = len(self.streams)
         cuda_streams = [torch.cuda.Stream(device=self.device) for _ in range(n)]
-        pending = [[] for _ in range(n)]     # arrived, not yet dispatched: (t_arrival, batch)
-        # in flight, oldest first: (event, t_arrival, batch, buffer); up to one
-        # per staging buffer of the beam's stream (two when double-buffered)
+        arrivals = []
+        for e in schedule:
+            t, b, k = e[:3]
+            extra = e[3] if len(e) > 3 else 0.0
+            drop = extra == DROPPED
+            arrivals.append((t if drop else t + float(extra), b, k, t, drop))
+        arrivals.sort(key=lambda a: a[0])
+        next_k = [None] * n                  # the batch each beam pushes next
+        for _, b, k, _, _ in arrivals:
+            next_k[b] = k if next_k[b] is None else min(next_k[b], k)
+        pending = [{} for _ in range(n)]     # arrived: batch -> (t actual, t nominal, dropped)
+        # in flight, oldest first: (event, batch, buffer, t actual, t nominal, dropped);
+        # up to one per staging buffer of the beam's stream
         inflight = [[] for _ in range(n)]
         report = ServeReport(deadline=deadline if deadline is not None
                              else max(s.cfg.period for s in self.streams),
@@ -267,22 +329,32 @@ class Server:
             return (time.perf_counter() - t0) * time_compression
 
         def finish(b):
-            ev, ta, k, idx = inflight[b].pop(0)
+            ev, k, idx, ta, tn, drop = inflight[b].pop(0)
             done = now()
+            if drop:
+                report.dropped.append((b, k))
+                return
             report.latencies.append((done - ta) / time_compression)
+            if done - tn > report.deadline * time_compression:
+                report.misses.append((b, k))
             report.dm_samples += self.streams[b].dm_samples
             if consumer is not None:
                 consumer(b, k, self.streams[b].outputs[idx])
 
         def dispatch(b):
             st = self.streams[b]
-            while pending[b] and len(inflight[b]) < st.nbuf:
-                ta, k = pending[b].pop(0)
-                source(b, k, st.staging)
+            while next_k[b] in pending[b] and len(inflight[b]) < st.nbuf:
+                k = next_k[b]
+                ta, tn, drop = pending[b].pop(k)
+                if drop:
+                    st.staging[...] = 0
+                else:
+                    source(b, k, st.staging)
                 idx = st.push(cuda_streams[b])
                 ev = torch.cuda.Event()
                 ev.record(cuda_streams[b])
-                inflight[b].append((ev, ta, k, idx))
+                inflight[b].append((ev, k, idx, ta, tn, drop))
+                next_k[b] = k + 1
 
         def poll():
             for b in range(n):
@@ -290,14 +362,20 @@ class Server:
                     finish(b)
                 dispatch(b)
 
-        for ta, b, k in schedule:
+        for ta, b, k, tn, drop in arrivals:
             while now() < ta:
                 poll()
                 time.sleep(0.0002)
-            pending[b].append((ta, k))
+            if ta > tn:
+                report.late.append((b, k))
+            pending[b][k] = (ta, tn, drop)
             poll()
-            dispatch(b)
         while any(inflight) or any(pending):
+            if not any(inflight) and all(next_k[b] not in pending[b] for b in range(n)
+                                         if pending[b]):
+                raise ValueError("schedule has a gap: batches "
+                                 f"{[(b, sorted(p)) for b, p in enumerate(pending) if p]} "
+                                 "wait for batches that never arrive")
             poll()
             time.sleep(0.0002)
         report.wall = (time.perf_counter() - t0)

@@ -276,11 +276,12 @@ dd_status dd_subband_dedispersion(const dd_observation *obs,
  * device array of about 1 MiB that every GPU loading the library keeps until
  * exit.  Limits: at most 4096 synthesized beams and 61440 live rows
  * (synthesized beams x non-zapped channels); larger requests return
- * DD_ERR_UNSUPPORTED.  The call enqueues on `stream` (a cudaStream_t) and
- * returns when the output is complete.  The first call on a device looks up
- * the array's address; make it before capturing any stream.  All calls share
- * the array, so calls that overlap on the GPU race (host threads are
- * serialized inside the call). */
+ * DD_ERR_UNSUPPORTED.  The call enqueues on `stream` (a cudaStream_t of the
+ * current device; another device's stream is DD_ERR_INVALID_ARGUMENT) and
+ * waits on it until the output is complete.  The first call on a device
+ * looks up the array's address, so that first call should come before any
+ * stream capture begins.  All calls share the array, so calls that overlap
+ * on the GPU race (host threads are serialized inside the call). */
 dd_status dd_dedispersion_noalloc(const dd_observation *obs,
                                   const uint32_t *zapped,
                                   const uint32_t *beam_mapping,
@@ -349,6 +350,15 @@ dd_status dd_plan_adds(const dd_plan *plan, uint64_t *adds);
  * (consecutive independent batches).  Applies to the shared-partial-sum and
  * 1/2/4/8-bit direct kernels; the 16-bit and float kernels launch as usual.
  * Off by default. */
+/* Limit, in nanoseconds, of each bounded device-side wait for a staged
+ * copy in this plan's runs (0, the default: 2 s).  When a wait runs out the
+ * kernel stops its tile, lets the copies it has in flight land, and the next
+ * dd_plan_check returns DD_ERR_TIMEOUT; the context stays usable.  A
+ * deliberately tiny limit exercises that path without a fault (the test of
+ * the timeout handling uses 1 ns); production code leaves it at 0.  No
+ * counterpart in the reference, whose host code reports OpenCL errors
+ * (src/DedispersionTuning.cpp:396-409). */
+dd_status dd_plan_set_wait_limit(dd_plan *plan, uint32_t ns);
 dd_status dd_plan_set_overlap(dd_plan *plan, int enable);
 dd_status dd_plan_destroy(dd_plan *plan);
 
@@ -546,6 +556,14 @@ dd_status dd_mlp_train(dd_mlp *mlp, const float *x, const float *target,
 dd_status dd_mlp_destroy(dd_mlp *mlp);
 
 /* ---- tuning support ------------------------------------------------------ */
+/* Measured add throughput of device `device`: streams of independent
+ * float adds and of 32-bit integer adds on every SM, timed with CUDA events,
+ * best of `repeats` runs (after one warm-up run); results in adds per second.
+ * It is the denominator of the path's add roofline (the direct sum is bound
+ * by adds, not by HBM).  No counterpart in the reference. */
+dd_status dd_measure_add_rate(int device, uint32_t repeats, double *fadd_per_s,
+                              double *iadd_per_s);
+
 /* Mean device time of `iterations` runs of a plan after `warmup` runs, timed
  * with CUDA events on a private stream (the reference's tuner times
  * enqueue + wait with a host timer, src/DedispersionTuning.cpp:384-395). */

@@ -19,13 +19,15 @@ from pathlib import Path
 
 import numpy as np
 
-from dedispersion_gb300._abi import DdConf, DdObservation
+from .types import DdConf, DdObservation  # noqa: F401  (re-exported for callers)
 
 HERE = Path(__file__).resolve().parent
 ORACLE_LIB = HERE / "libddoracle.so"
 REF_LIB = HERE / "_ref" / "libddref.so"
 
-_OBS = C.POINTER(DdObservation)
+# Structs are passed by address: either oracle.types' mirrors or the engine's
+# own structs of the same layout.
+_OBS = C.c_void_p
 _U32P = C.POINTER(C.c_uint32)
 _F32P = C.POINTER(C.c_float)
 _F64P = C.POINTER(C.c_double)
@@ -42,8 +44,32 @@ def _u32(a):
     return a.ctypes.data_as(_U32P)
 
 
-def build() -> None:
+def reference_sources() -> Path | None:
+    """Where the reference's sources are: $DD_REFERENCE, else the location
+    oracle/Makefile names; None when neither holds include/Dedispersion.hpp
+    (always the case on a machine without the reference checkout)."""
+    src = os.environ.get("DD_REFERENCE")
+    if not src:
+        proc = subprocess.run(["make", "-s", "--no-print-directory", "-C", str(HERE),
+                               "print-reference"], capture_output=True, text=True)
+        src = proc.stdout.strip() if proc.returncode == 0 else ""
+    if src and (Path(src) / "include" / "Dedispersion.hpp").exists():
+        return Path(src)
+    return None
+
+
+def build(reference: bool = False, verbose: bool = False) -> None:
+    """Compile the restatement (oracle/libddoracle.so); with reference=True
+    also the reference's own CPU code (oracle/_ref/libddref.so) where its
+    sources are present.  Test infrastructure: the engine never calls this."""
     subprocess.run(["make", "-s", "-C", str(HERE), "all"], check=True)
+    if reference:
+        src = reference_sources()
+        if src is not None:
+            subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REFERENCE={src}"],
+                           check=True)
+    if verbose:
+        print("built oracle" + (" and oracle/_ref" if REF_LIB.exists() else ""))
 
 
 def restated() -> C.CDLL:
@@ -77,10 +103,7 @@ def reference() -> C.CDLL | None:
     global _ref
     if _ref is None:
         if not REF_LIB.exists():
-            ref_src = Path(os.environ.get("DD_REFERENCE", "/root/reference"))
-            if (ref_src / "include" / "Dedispersion.hpp").exists():
-                subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REFERENCE={ref_src}"],
-                               check=True)
+            build(reference=True)
         if not REF_LIB.exists():
             return None
         h = C.CDLL(str(REF_LIB))
@@ -93,7 +116,7 @@ def reference() -> C.CDLL | None:
                                         C.c_size_t, _F32P, C.c_size_t, C.c_uint]
         h.ddref_step_two.argtypes = [_OBS, _U32P, C.c_size_t, _F32P, C.c_size_t, _F32P,
                                      C.c_size_t, _F32P, C.c_size_t, C.c_uint]
-        h.ddref_read_tuned_conf.argtypes = [C.c_char_p, C.c_char_p, C.c_uint, C.POINTER(DdConf),
+        h.ddref_read_tuned_conf.argtypes = [C.c_char_p, C.c_char_p, C.c_uint, C.c_void_p,
                                             C.c_char_p, C.c_size_t]
         _ref = h
     return _ref

@@ -208,3 +208,50 @@ def test_time_major_double_buffered_stream(gpu):
             want, got_idx = [], []
     a.close()
     b.close()
+
+
+@pytest.mark.gpu
+def test_late_and_dropped_batches(gpu):
+    """Faults injected on the host: beam 0's batch 1 arrives 0.12 s late (its
+    deadline is 0.05 s after its nominal arrival), beam 1's batch 2 never
+    arrives.  The late batch and the batch queued behind it miss their
+    deadlines, the next one does not; the dropped batch is pushed as zeros,
+    neither delivered nor timed, and every delivered batch still equals the
+    plain path on its window (the ring stays aligned in time)."""
+    pytest.importorskip("torch")
+    period = 0.05
+    beams = small_beams()[:2]
+    server = serving.Server(budget_bytes=150 * 10**9)
+    for cfg in beams:
+        server.admit(cfg)
+    nb = 4
+    schedule = [(k * period + 0.001 * b, b, k) for k in range(nb) for b in range(len(beams))]
+    schedule = serving.inject(schedule, late={(0, 1): 0.12}, dropped=[(1, 2)])
+    inputs, outputs = {}, {}
+
+    def source(b, k, staging):
+        data = batch_data(beams[b], k)
+        staging[:, :data.shape[1]] = data
+        inputs[(b, k)] = data
+
+    def consumer(b, k, out):
+        outputs[(b, k)] = out.copy()
+
+    report = server.serve(schedule, source, consumer, deadline=period)
+    s = report.summary()
+    assert s["batches"] == len(beams) * nb - 1 and s["dropped_batches"] == 1
+    assert report.dropped == [(1, 2)] and report.late == [(0, 1)]
+    assert set(report.misses) == {(0, 1), (0, 2)}, report.misses
+    assert (1, 2) not in outputs and (1, 2) not in inputs
+    for b, stream in enumerate(server.streams):
+        cfg = stream.cfg
+        prev = np.zeros((cfg.channels, stream.tail), np.uint8)
+        for k in range(nb):
+            cur = inputs.get((b, k), np.zeros((cfg.channels, cfg.samples), np.uint8))
+            window = np.concatenate([prev, cur], axis=1)
+            if (b, k) in outputs:
+                want = plain_reference(stream, window)
+                assert np.array_equal(outputs[(b, k)].view(np.uint32),
+                                      want.view(np.uint32)), (cfg.name, k)
+            prev = window[:, window.shape[1] - stream.tail:] if stream.tail else prev
+    server.close()

@@ -58,6 +58,8 @@ def test_noalloc_matches_plan_on_two_calls_in_a_row(gpu):
         want = plan_output(torch, case, d_in)
         # garbage in the output buffer must be overwritten wherever it is defined
         d_out = torch.full((case.out_elems,), -7.0, dtype=torch.float32, device="cuda")
+        # the fill and the copy above ran on torch's current stream
+        stream.wait_stream(torch.cuda.current_stream())
         rc = noalloc(case, d_in, d_out, stream.cuda_stream)
         assert rc == 0, _abi.lib().dd_last_error().decode()
         got = d_out.cpu().numpy()
@@ -80,3 +82,15 @@ def test_noalloc_rejects_requests_beyond_its_limit(gpu):
         case.shifts.ctypes.data_as(F32P), 0, 8, None)
     assert rc == _abi.DD_ERR_UNSUPPORTED
     assert "no-alloc limit" in _abi.lib().dd_last_error().decode()
+    # under the beam limit, over the 61440 live rows: 16 beams x 4096 channels
+    wide = single_case(C=4096, D=8, S=64, bits=8, padding=0, zap=0.0, seed=34)
+    many = wide.obs.copy()
+    many.setNrSynthesizedBeams(16)
+    mapping = np.zeros(16 * 4096, np.uint32)
+    rc = _abi.lib().dd_dedispersion_noalloc(
+        C.byref(many.c), wide.zapped.ctypes.data_as(U32P), mapping.ctypes.data_as(U32P),
+        C.c_void_p(d_in.data_ptr()), C.cast(C.c_void_p(d_out.data_ptr()), F32P),
+        wide.shifts.ctypes.data_as(F32P), 0, 8, None)
+    assert rc == _abi.DD_ERR_UNSUPPORTED
+    msg = _abi.lib().dd_last_error().decode()
+    assert "65536 live rows" in msg and "no-alloc limit of 61440" in msg
