@@ -145,11 +145,6 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
-// The bounded wait's limit of a problem (ProblemDesc::wait_ns, else 2 s).
-__device__ __forceinline__ unsigned long long wait_limit(const ProblemDesc &P) {
-  return P.wait_ns ? (unsigned long long)P.wait_ns : kWaitNs;
-}
-
 // Non-blocking test of the phase with `parity`.
 __device__ __forceinline__ bool mbar_test_wait(uint64_t *bar, uint32_t parity) {
   uint32_t ok;
@@ -163,14 +158,19 @@ __device__ __forceinline__ bool mbar_test_wait(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait for the phase with `parity` to complete.  A limit below a
-// microsecond is one non-blocking test (try_wait may itself suspend for
-// about that long), so that such a limit reliably runs out on a copy that
-// has not landed yet.
+// Bounded wait for the phase with `parity` to complete.  `test_ns` is the
+// problem's override of the limit (ProblemDesc::wait_ns, 0: `limit_ns`),
+// read only once the first try has failed so that the common path stays
+// as short as it was; an override below a microsecond gives up right after
+// that first try.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
-                                          unsigned long long limit_ns) {
-  if (limit_ns < 1000ull) return mbar_test_wait(bar, parity);
+                                          unsigned long long limit_ns,
+                                          uint32_t test_ns = 0) {
   if (mbar_try_wait(bar, parity)) return true;
+  if (test_ns) {
+    if (test_ns < 1000u) return false;
+    limit_ns = test_ns;
+  }
   const unsigned long long start = global_ns();
   for (;;) {
 #pragma unroll 1
@@ -345,6 +345,27 @@ __device__ __forceinline__ void drain_stages(const StageCtx &S, uint32_t sc,
   }
 }
 
+// Test hook of the timeout path (ProblemDesc::wait_ns of 1..999 ns), right
+// after the prologue has issued stages [0, pro): one non-blocking test of
+// stage 0's barrier.  A copy that has not landed yet -- the common case this
+// early -- sends the CTA down the path a wait that runs out takes: the status
+// bit, a bounded drain of the stages in flight, an early return (true).  It
+// sits outside the stage loop, so the loop's code is the same with or
+// without it.
+__device__ __forceinline__ bool timeout_test_hook(const ProblemDesc &P, const StageCtx &S,
+                                                  uint32_t sc, uint32_t pro) {
+  const bool ok = mbar_test_wait(S.bars + sc % kNRaw, (sc / kNRaw) & 1u);
+  if (!__syncthreads_or(!ok)) return false;
+  if (threadIdx.x == 0) atomicOr(P.status, kStatusTimeout);
+  drain_stages(S, sc, 0, pro);
+  return true;
+}
+
+// Whether a problem asks for the timeout test hook.
+__device__ __forceinline__ bool timeout_test(const ProblemDesc &P) {
+  return P.wait_ns - 1u < 999u;
+}
+
 // ---- swar8 tile -----------------------------------------------------------
 
 // Inner-loop variants of the swar8 family.  Both keep sums exact.
@@ -415,6 +436,9 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
     for (uint32_t s = 0; s < pro; ++s)
       issue_stage<CH>(P, G, S, s, sc + s, t0, d0, dtile, tx);
   }
+  if (timeout_test(P) && nst &&
+      timeout_test_hook(P, S, sc, nst < (uint32_t)kNRaw ? nst : (uint32_t)kNRaw))
+    return false;
 
   // kUnpackPermute: lo = (b0, b1) lanes, hi = (b2, b3) lanes.
   // kUnpackMaskHigh: lo = E (b0, b2 lanes), hi = A (w >> 8 sum).
@@ -456,7 +480,7 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
   for (uint32_t s = 0; s < nst; ++s) {
     const uint32_t gs = sc + s, slot = gs % kNRaw, area = gs & 1u;
     const uint32_t cnt = (K - s * CH) < (uint32_t)CH ? (K - s * CH) : CH;
-    const bool ok = mbar_wait(S.bars + slot, (gs / kNRaw) & 1u, wait_limit(P));
+    const bool ok = mbar_wait(S.bars + slot, (gs / kNRaw) & 1u, kWaitNs, P.wait_ns);
     if (!P.tma) {
       copy_stage_plain<CH, TY>(P, G, S, s, slot, cnt);
       __syncthreads();
@@ -688,6 +712,9 @@ __device__ __forceinline__ bool scalar_tile(const ProblemDesc &P,
     for (uint32_t s = 0; s < pro; ++s)
       issue_stage<CH>(P, G, S, s, sc + s, t0, d0, dtile, tx);
   }
+  if (timeout_test(P) && nst &&
+      timeout_test_hook(P, S, sc, nst < (uint32_t)kAhead ? nst : (uint32_t)kAhead))
+    return false;
 
   Acc acc[NDT][NS];
 #pragma unroll
@@ -701,7 +728,7 @@ __device__ __forceinline__ bool scalar_tile(const ProblemDesc &P,
   for (uint32_t s = 0; s < nst; ++s) {
     const uint32_t gs = sc + s, slot = gs % kNRaw, area = gs & 1u;
     const uint32_t cnt = (K - s * CH) < (uint32_t)CH ? (K - s * CH) : CH;
-    const bool ok = mbar_wait(S.bars + slot, (gs / kNRaw) & 1u, wait_limit(P));
+    const bool ok = mbar_wait(S.bars + slot, (gs / kNRaw) & 1u, kWaitNs, P.wait_ns);
     if (!P.tma) {
       copy_stage_plain<CH, TY>(P, G, S, s, slot, cnt);
       __syncthreads();
@@ -793,6 +820,9 @@ __device__ __forceinline__ bool pair_tile(const ProblemDesc &P, uint32_t g,
     for (uint32_t s = 0; s < pro; ++s)
       issue_stage<CH>(P, G, S, s, sc + s, t0, d0, dtile, tx);
   }
+  if (timeout_test(P) && nst &&
+      timeout_test_hook(P, S, sc, nst < (uint32_t)kAhead ? nst : (uint32_t)kAhead))
+    return false;
 
   uint32_t acc[NDT][NS], tlo[NDT][NS], thi[NDT][NS];
 #pragma unroll
@@ -817,7 +847,7 @@ __device__ __forceinline__ bool pair_tile(const ProblemDesc &P, uint32_t g,
   for (uint32_t s = 0; s < nst; ++s) {
     const uint32_t gs = sc + s, slot = gs % kNRaw, area = gs & 1u;
     const uint32_t cnt = (K - s * CH) < (uint32_t)CH ? (K - s * CH) : CH;
-    const bool ok = mbar_wait(S.bars + slot, (gs / kNRaw) & 1u, wait_limit(P));
+    const bool ok = mbar_wait(S.bars + slot, (gs / kNRaw) & 1u, kWaitNs, P.wait_ns);
     if (!P.tma) {
       copy_stage_plain<CH, TY>(P, G, S, s, slot, cnt);
       __syncthreads();

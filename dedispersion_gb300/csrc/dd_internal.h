@@ -129,9 +129,10 @@ struct ProblemDesc {
   uint32_t flush_rows;    // rows summed in 16-bit lanes before widening
   uint64_t pair_stride;   // floats from a coarse DM 2p row to its 2p + 1 row
   // Limit of each bounded wait for a staged copy, in ns (0: the default of
-  // 2 s).  A tiny limit makes the waits run out: the test of the timeout
-  // path sets it (dd_plan_set_wait_limit).  The drain after a timeout keeps
-  // its own limit, so every copy in flight lands before a CTA exits.
+  // 2 s; below 1000: give up as soon as the first test of the barrier finds
+  // the copy not landed).  The test of the timeout path sets it
+  // (dd_plan_set_wait_limit).  The drain after a timeout keeps its own
+  // limit, so every copy in flight lands before a CTA exits.
   uint32_t wait_ns;
 };
 

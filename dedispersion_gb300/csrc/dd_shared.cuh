@@ -240,10 +240,14 @@ __device__ __forceinline__ bool shared8_tile(const ProblemDesc &P, uint32_t g_in
       (void)mbar_wait(bars + (sc + u) % kSharedSlots, ((sc + u) / kSharedSlots) & 1u, kDrainNs);
     return false;
   };
+  // Test hook of the timeout path (timeout_test_hook in dd_device.cuh).
+  if (timeout_test(P) && nst &&
+      __syncthreads_or(!mbar_test_wait(bars + sc % kSharedSlots, (sc / kSharedSlots) & 1u)))
+    return abort(0);
 
   for (uint32_t s = 0; s < nst; ++s) {
     const uint32_t gs = sc + s, slot = gs % kSharedSlots;
-    const bool ok = mbar_wait(bars + slot, (gs / kSharedSlots) & 1u, wait_limit(P));
+    const bool ok = mbar_wait(bars + slot, (gs / kSharedSlots) & 1u, kWaitNs, P.wait_ns);
     const uint16_t *tb =
         reinterpret_cast<const uint16_t *>(smem + L.off_table + slot * P.table_bytes);
     uint8_t *rs = smem + L.off_raw + slot * kStageRows * L.raw_bytes;

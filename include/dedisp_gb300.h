@@ -353,9 +353,10 @@ dd_status dd_plan_adds(const dd_plan *plan, uint64_t *adds);
 /* Limit, in nanoseconds, of each bounded device-side wait for a staged
  * copy in this plan's runs (0, the default: 2 s).  When a wait runs out the
  * kernel stops its tile, lets the copies it has in flight land, and the next
- * dd_plan_check returns DD_ERR_TIMEOUT; the context stays usable.  A
- * deliberately tiny limit exercises that path without a fault (the test of
- * the timeout handling uses 1 ns); production code leaves it at 0.  No
+ * dd_plan_check returns DD_ERR_TIMEOUT; the context stays usable.  A limit
+ * below 1000 ns gives up as soon as the first test finds a copy not yet
+ * landed: that exercises the path without a fault (the test of the timeout
+ * handling uses 1 ns); production code leaves the limit at 0.  No
  * counterpart in the reference, whose host code reports OpenCL errors
  * (src/DedispersionTuning.cpp:396-409). */
 dd_status dd_plan_set_wait_limit(dd_plan *plan, uint32_t ns);
