@@ -69,6 +69,8 @@ def parse():
                     help="skip the 40-beam batched measurement")
     ap.add_argument("--no-served", action="store_true",
                     help="skip the 12-beam serving measurement")
+    ap.add_argument("--no-tuning", action="store_true",
+                    help="skip the learned-tuner measurement (400-shape sweep and training)")
     ap.add_argument("--kernel", default=None,
                     help="registry name of the tile configuration to run (default: the "
                          "library's default for the workload)")
@@ -846,6 +848,10 @@ def main():
     subband = bench_subband(torch, local, max(10, min(args.steps, 50)), hbm_peak, peak_adds)
     float32 = bench_float(torch, local, max(3, min(args.steps, 10)), peak_adds)
     batched = bench_batched(torch, local, peak_adds=peak_adds) if not args.no_batched else None
+    tuning_line = None
+    if not args.no_tuning:
+        from dedispersion_gb300 import tuning
+        tuning_line = tuning.bench_report(device=local)
 
     if rank != 0:
         return
@@ -910,6 +916,7 @@ def main():
         "float32": float32,
         "batched": batched,
         "served": served,
+        "tuning": tuning_line,
     }
     print(json.dumps(line), flush=True)
     if pg is not None:

@@ -225,12 +225,14 @@ class StudyRecord:
 
 
 def collect(shapes: list[Shape], padding: int = 128, iterations: int = 3, device: int = 0,
-            log=None) -> list[StudyRecord]:
-    """Time every configuration of every shape (the exhaustive sweep)."""
+            log=None, full_size: bool = False) -> list[StudyRecord]:
+    """Time every configuration of every shape (the exhaustive sweep), each
+    cut as measured_observation cuts it, or at its full size."""
     import torch
     records = []
     for i, s in enumerate(shapes):
-        obs = measured_observation(s, padding)
+        obs = (measured_observation(s, padding, max_dms=s.dms, max_samples=s.samples)
+               if full_size else measured_observation(s, padding))
         mode = s.mode()
         shifts = getShifts(obs, padding)
         zapped = syn.zapped_mask(s.channels, 0.05, s.seed, padding)
@@ -404,8 +406,102 @@ def study(count: int = 400, train_fraction: float = 0.8, steps: int = 3000, k: i
     return rep
 
 
+def direct_sum_adds(s: Shape) -> float:
+    """Direct-sum adds of a shape at full size (its single-step work)."""
+    return float(s.channels) * s.dms * s.samples
+
+
+def bench_report(count: int = 400, k: int = 2, steps: int = 3000, device: int = 0,
+                 full_shapes: int = 2, max_full_adds: float = 2e11) -> dict:
+    """The learned tuner measured for a benchmark line: the study's sweep of
+    `count` seeded shapes (cut to <= 256 DMs x 8192 samples), the model
+    trained on 80 % of them, its top-k against the exhaustive best on the
+    held-out 20 % (k = 1, 2, 4), and the same at full size on the
+    1536-channel x 2048-DM x 24576-sample workload (single step and 32
+    subbands) plus `full_shapes` held-out shapes of at most `max_full_adds`
+    direct-sum adds, each swept exhaustively at full size."""
+    t0 = time.perf_counter()
+    shapes = study_shapes(count)
+    records = collect(shapes, device=device)
+    t_collect = time.perf_counter() - t0
+    perm = np.random.default_rng(1).permutation(len(records))
+    n_train = int(round(0.8 * len(records)))
+    train_idx, test_idx = perm[:n_train], perm[n_train:]
+    X, y, owner = dataset(records)
+    mask = np.isin(owner, train_idx)
+    tuner = LearnedTuner(device=device)
+    t0 = time.perf_counter()
+    tuner.fit(X[mask], y[mask], steps=steps)
+    t_train = time.perf_counter() - t0
+    keys = ("top_k_vs_best_mean", "top_k_vs_best_median", "top_k_vs_best_worst",
+            "shapes_within_5pct", "random_k_vs_best_mean", "default_vs_best_mean",
+            "tuning_time_ratio")
+    by_k = {str(kk): {key: v for key, v in evaluate(records, tuner, test_idx, k=kk).items()
+                      if key in keys} for kk in (1, 2, 4)}
+    # full size: the benchmark workload in both modes, and small held-out shapes
+    full = [Shape(channels=1536, dms=2048, samples=24576, bits=8, subbands=0, dm_step=0.2,
+                  seed=11),
+            Shape(channels=1536, dms=2048, samples=24576, bits=8, subbands=32, dm_step=0.2,
+                  seed=12)]
+    picked = [shapes[i] for i in test_idx if direct_sum_adds(shapes[i]) <= max_full_adds]
+    full += picked[:full_shapes]
+    t0 = time.perf_counter()
+    full_records = collect(full, device=device, full_size=True)
+    t_full = time.perf_counter() - t0
+    full_rep = {str(kk): evaluate(full_records, tuner, range(len(full_records)), k=kk)
+                for kk in (1, 2, 4)}
+    return {"k": k, "held_out": {"shapes": len(test_idx), **by_k[str(k)]},
+            "by_k": by_k,
+            "full_size": {"shapes": [f"{s.channels} ch x {s.dms} DM x {s.samples} samples, "
+                                     f"{s.bits}-bit, {s.subbands} subbands, step {s.dm_step:.3f}"
+                                     for s in full],
+                          "by_k": {kk: {key: v for key, v in r.items() if key in keys}
+                                   for kk, r in full_rep.items()},
+                          "sweep_s": t_full},
+            "study_shapes": count, "train_rows": int(mask.sum()), "collect_s": t_collect,
+            "train_s": t_train,
+            "network": "3 x 128 ReLU, bf16 weights, fp32 accumulation, trained by the "
+                       "library's CUDA kernels (Adam, full batch)",
+            "what": "held-out shapes are cut to <= 256 DMs x 8192 samples for timing; "
+                    "full_size shapes are timed whole; tuning time = building and timing the "
+                    "chosen configurations plus ranking, against the same for all of them"}
+
+
 # ---------------------------------------------------------------------------
 # command line: the reference's DedispersionTuning switches
+
+def registry_filter(candidates, mode: int, bits: int, a) -> list:
+    """The reference tuner's limits on its enumeration
+    (src/DedispersionTuning.cpp:201-283) applied to the compiled registry:
+    threadsD0 from -min_threads up to -max_columns, threadsD1 up to -max_rows,
+    threadsD0 x threadsD1 at most -max_threads and a multiple of -vector,
+    itemsD0 up to -max_sample_items, itemsD1 up to -max_dm_items, unroll up
+    to -max_unroll, and the reference's register estimate of a
+    local-memory kernel, itemsD1 + itemsD0 x itemsD1 + 9 (single step) or
+    + 10 (step one, two), + 4 below 8 bits, at most -max_items.  An unset
+    switch (None or 0) does not filter."""
+    out = []
+    for k in candidates:
+        c = k.conf
+        t0, t1 = c.nrThreadsD0, c.nrThreadsD1
+        est = c.nrItemsD1 + c.nrItemsD0 * c.nrItemsD1 + (9 if mode == DD_SINGLE_STEP else 10)
+        if bits < 8:
+            est += 4
+        checks = (
+            (getattr(a, "min_threads", None), lambda v: t0 >= v),
+            (getattr(a, "max_columns", None), lambda v: t0 <= v),
+            (getattr(a, "max_rows", None), lambda v: t1 <= v),
+            (getattr(a, "max_threads", None), lambda v: t0 * t1 <= v),
+            (getattr(a, "vector", None), lambda v: (t0 * t1) % v == 0),
+            (getattr(a, "max_sample_items", None), lambda v: c.nrItemsD0 <= v),
+            (getattr(a, "max_dm_items", None), lambda v: c.nrItemsD1 <= v),
+            (getattr(a, "max_unroll", None), lambda v: c.unroll <= v),
+            (getattr(a, "max_items", None), lambda v: est <= v),
+        )
+        if all(ok(v) for v, ok in checks if v):
+            out.append(k)
+    return out
+
 
 def _args(argv):
     ap = argparse.ArgumentParser(prog="python -m dedispersion_gb300.tuning",
@@ -419,7 +515,9 @@ def _args(argv):
                       ("-subbanding_dms", int), ("-subbanding_dm_first", float),
                       ("-subbanding_dm_step", float), ("-input_bits", int),
                       ("-min_threads", int), ("-max_threads", int), ("-max_items", int),
-                      ("-max_unroll", int)):
+                      ("-max_unroll", int), ("-max_rows", int), ("-max_columns", int),
+                      ("-vector", int), ("-max_sample_items", int), ("-max_dm_items", int),
+                      ("-opencl_platform", int), ("-opencl_device", int)):
         ap.add_argument(flag, type=typ)
     ap.add_argument("-zapped_channels")
     ap.add_argument("-device_name", default="GB300")
@@ -480,20 +578,7 @@ def main(argv=None) -> int:
         o.setNrSamplesPerDispersedBatch(syn.dispersed_samples(
             s1, shifts[0], a.subbanding_dm_first or 0.0, a.subbanding_dms,
             a.subbanding_dm_step or 0.0), True)
-    cands = []
-    for k in family_kernels(mode, bits):
-        c = k.conf
-        threads = c.nrThreadsD0 * c.nrThreadsD1
-        items = c.nrItemsD0 * c.nrItemsD1
-        if a.min_threads and threads < a.min_threads:
-            continue
-        if a.max_threads and threads > a.max_threads:
-            continue
-        if a.max_items and items > a.max_items:
-            continue
-        if a.max_unroll and c.unroll > a.max_unroll:
-            continue
-        cands.append(k)
+    cands = registry_filter(family_kernels(mode, bits), mode, bits, a)
     if a.learned and not a.step_two:
         # time only the cost model's top k (step two has no model: full sweep)
         tuner = LearnedTuner.load(a.learned)

@@ -35,6 +35,34 @@ def test_features_distinguish_configurations(engine):
         assert f[-nf - nv:-nf].sum() == (1 if k.name.startswith("swar8") else 0), k.name
 
 
+def test_reference_switches_filter_the_registry(engine):
+    """-max_rows/-max_columns/-vector/-max_sample_items/-max_dm_items/
+    -max_unroll/-max_items/-min_threads/-max_threads keep exactly the
+    configurations the reference's enumeration limits would admit
+    (src/DedispersionTuning.cpp:201-283)."""
+    import argparse
+    ks = tuning.family_kernels(dd.DD_SINGLE_STEP, 8)
+    none = argparse.Namespace()
+    assert tuning.registry_filter(ks, dd.DD_SINGLE_STEP, 8, none) == ks
+    a = tuning._args(["-single_step", "-max_rows", "8", "-max_columns", "32", "-vector", "64",
+                      "-max_sample_items", "8", "-max_dm_items", "4", "-max_unroll", "16",
+                      "-max_items", "40", "-min_threads", "32", "-max_threads", "1024"])
+    kept = tuning.registry_filter(ks, dd.DD_SINGLE_STEP, 8, a)
+    assert kept and len(kept) < len(ks)
+    for k in ks:
+        c = k.conf
+        t0, t1 = c.nrThreadsD0, c.nrThreadsD1
+        est = c.nrItemsD1 + c.nrItemsD0 * c.nrItemsD1 + 9
+        ok = (32 <= t0 <= 32 and t1 <= 8 and t0 * t1 <= 1024 and (t0 * t1) % 64 == 0 and
+              c.nrItemsD0 <= 8 and c.nrItemsD1 <= 4 and c.unroll <= 16 and est <= 40)
+        assert (k in kept) == ok, k.name
+    # sub-byte input adds 4 to the register estimate
+    tight = tuning._args(["-single_step", "-max_items", str(min(
+        k.conf.nrItemsD1 + k.conf.nrItemsD0 * k.conf.nrItemsD1 + 9 for k in ks))])
+    assert tuning.registry_filter(ks, dd.DD_SINGLE_STEP, 8, tight)
+    assert not tuning.registry_filter(ks, dd.DD_SINGLE_STEP, 4, tight)
+
+
 @pytest.mark.gpu
 def test_exhaustive_cli_best_line(gpu, tmp_path):
     tuned = tmp_path / "tuned.conf"
