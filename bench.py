@@ -77,6 +77,12 @@ def parse():
     ap.add_argument("--kernel-only", action="store_true",
                     help="run only the warm-up and timed kernel launches (the command ncu "
                          "captures); prints the device-resident figure alone")
+    ap.add_argument("--float-only", action="store_true",
+                    help="run only the float32-input line (--steps runs after 2 warm-up runs; "
+                         "the command ncu captures for the float kernel)")
+    ap.add_argument("--float-kernel", default=None,
+                    help="registry name of the float tile for the float32 line (default: the "
+                         "library's float default)")
     ap.add_argument("--subband-only", type=int, default=None, metavar="CHUNKS",
                     help="run only the subband pipeline, --warmup + --steps runs with "
                          "dd_subband_set_chunks(CHUNKS) (the command ncu captures for the "
@@ -336,7 +342,7 @@ def bench_ingest(torch, inp, lay, obs, stream):
                     "descending-frequency file order reversed on the way"}
 
 
-def bench_float(torch, device: int, steps: int, peak_adds: float):
+def bench_float(torch, device: int, steps: int, peak_adds: float, kernel: str | None = None):
     """Config 2 with float32 input (N(128, 20), same channels, DMs, zapping):
     throughput of the float path (summed in the reference's channel order),
     and its largest relative error against an FP64 sum of four DM rows
@@ -356,7 +362,12 @@ def bench_float(torch, device: int, steps: int, peak_adds: float):
     d_in = torch.zeros((C, row), dtype=torch.float32, device=f"cuda:{device}")
     d_in[:, :n] = torch.randn((C, n), generator=g, device=f"cuda:{device}") * 20.0 + 128.0
     d_out = torch.empty(lay.output_bytes // 4, dtype=torch.float32, device=f"cuda:{device}")
-    p = dd.Plan(obs, dd.DD_SINGLE_STEP, 32, PADDING, device=device)
+    kidx = None
+    if kernel:
+        kidx = next((k.index for k in dd.kernels() if k.name == kernel), None)
+        if kidx is None:
+            raise SystemExit(f"no compiled configuration named {kernel}")
+    p = dd.Plan(obs, dd.DD_SINGLE_STEP, 32, PADDING, device=device, kernel=kidx)
     p.setShifts(shifts)
     p.setZappedChannels(zapped)
     p.setBeamMapping(mapping)
@@ -383,11 +394,13 @@ def bench_float(torch, device: int, steps: int, peak_adds: float):
         for c, dl in zip(live, delay):
             ref += host[c, dl:dl + S]
         err = max(err, float(np.max(np.abs(out[d] - ref) / np.abs(ref))))
+    kernel = next((k.name for k in dd.kernels()
+                   if k.elem_bits == 32 and k.conf.print() == p.conf().print()), "?")
     p.close()
     adds = D * S * len(live)
     return {"value": D * S / t, "unit": UNIT, "ms_per_step": t * 1e3, "dtype": "f32",
             "adds_frac": adds / t / peak_adds, "max_rel_err_vs_fp64": err,
-            "tolerance": 1e-5, "kernel": "scalar float tile",
+            "tolerance": 1e-5, "kernel": kernel,
             "workload": "1536 ch x 2048 DM x 24576 samples, float32 N(128, 20), 5% zapped"}
 
 
@@ -736,6 +749,12 @@ def main():
     import torch
     import dedispersion_gb300 as dd
     torch.cuda.set_device(local)
+    if args.float_only:
+        rates = dd.measure_add_rate(local, 2)
+        print(json.dumps(bench_float(torch, local, args.steps,
+                                     max(rates["fadd_per_s"], rates["iadd_per_s"]),
+                                     args.float_kernel)))
+        return
     if args.subband_only is not None:
         print(json.dumps(subband_only(torch, local, args.subband_only, args.steps, args.warmup)))
         return
@@ -846,7 +865,7 @@ def main():
     served = bench_served(local, peak_adds=peak_adds) if not args.no_served else None
     ingest_line = bench_ingest(torch, inp, lay, obs, stream)
     subband = bench_subband(torch, local, max(10, min(args.steps, 50)), hbm_peak, peak_adds)
-    float32 = bench_float(torch, local, max(3, min(args.steps, 10)), peak_adds)
+    float32 = bench_float(torch, local, max(3, min(args.steps, 10)), peak_adds, args.float_kernel)
     batched = bench_batched(torch, local, peak_adds=peak_adds) if not args.no_batched else None
     tuning_line = None
     if not args.no_tuning:
