@@ -10,8 +10,11 @@ step, or step one then step two --, copy out, carry the tail).  The server:
   refused with DD_ERR_OVER_BUDGET;
 * runs a schedule of batch arrivals (per beam a batch every period, delayed
   by an exponential jitter -- Poisson-jittered arrivals), one CUDA stream per
-  beam so that beams overlap on the GPU, at most one batch in flight per beam
-  and later arrivals of a busy beam queued;
+  beam so that beams overlap on the GPU, one batch in flight per staging
+  buffer of a beam (two when double-buffered) and later arrivals of a busy
+  beam queued; the beams' host staging copies run on a pool of threads;
+* injects host-side faults on request (:func:`inject`): late batches and
+  batches whose data never arrive (pushed as zeros, counted as dropped);
 * reports per-batch latency (arrival -> output in host memory), p50/p99
   against the deadline (the batch period), and throughput in DM-samples/s.
 
@@ -287,7 +290,7 @@ class Server:
         self.used = 0
 
     def serve(self, schedule, source, consumer=None, time_compression: float = 1.0,
-              deadline: float | None = None) -> ServeReport:
+              deadline: float | None = None, workers: int | None = None) -> ServeReport:
         """Run `schedule`: entries (arrival s, beam, batch), or (nominal
         arrival s, beam, batch, delay s or DROPPED) as :func:`inject` makes
         them.  source(beam, batch, staging) fills a beam's pinned staging
@@ -302,9 +305,20 @@ class Server:
         timed.  Latency runs from a batch's actual arrival to its output on
         the host; a batch misses its deadline when its output lands more
         than `deadline` (default: the longest batch period) after its
-        nominal arrival."""
+        nominal arrival.
+
+        Staging a batch (the source's copy into pinned memory) and its push
+        run on a pool of `workers` host threads (default: one per beam, at
+        most 8), one batch of a beam at a time, so that the beams' host
+        copies overlap each other and the GPU's work, as the beams' receiver
+        threads would in a telescope's pipeline."""
+        import os
+        from concurrent.futures import ThreadPoolExecutor
+
         import torch
         n = len(self.streams)
+        if workers is None:
+            workers = max(1, min(n, 8, os.cpu_count() or 1))
         cuda_streams = [torch.cuda.Stream(device=self.device) for _ in range(n)]
         arrivals = []
         for e in schedule:
@@ -317,12 +331,28 @@ class Server:
         for _, b, k, _, _ in arrivals:
             next_k[b] = k if next_k[b] is None else min(next_k[b], k)
         pending = [{} for _ in range(n)]     # arrived: batch -> (t actual, t nominal, dropped)
-        # in flight, oldest first: (event, batch, buffer, t actual, t nominal, dropped);
-        # up to one per staging buffer of the beam's stream
+        # in flight on the GPU, oldest first: (event, batch, buffer, t actual,
+        # t nominal, dropped); up to one per staging buffer of the beam's stream
         inflight = [[] for _ in range(n)]
+        staging = [None] * n                 # the beam's batch being staged: (future, ...)
         report = ServeReport(deadline=deadline if deadline is not None
                              else max(s.cfg.period for s in self.streams),
                              time_compression=time_compression)
+        device = self.device
+
+        def stage_and_push(b, k, drop):
+            torch.cuda.set_device(device)
+            st = self.streams[b]
+            if drop:
+                st.staging[...] = 0
+            else:
+                source(b, k, st.staging)
+            idx = st.push(cuda_streams[b])
+            ev = torch.cuda.Event()
+            ev.record(cuda_streams[b])
+            return ev, idx
+
+        pool = ThreadPoolExecutor(max_workers=workers)
         t0 = time.perf_counter()
 
         def now():
@@ -342,18 +372,18 @@ class Server:
                 consumer(b, k, self.streams[b].outputs[idx])
 
         def dispatch(b):
+            if staging[b] is not None:
+                fut, k, ta, tn, drop = staging[b]
+                if not fut.done():
+                    return
+                ev, idx = fut.result()
+                inflight[b].append((ev, k, idx, ta, tn, drop))
+                staging[b] = None
             st = self.streams[b]
-            while next_k[b] in pending[b] and len(inflight[b]) < st.nbuf:
+            if next_k[b] in pending[b] and len(inflight[b]) < st.nbuf:
                 k = next_k[b]
                 ta, tn, drop = pending[b].pop(k)
-                if drop:
-                    st.staging[...] = 0
-                else:
-                    source(b, k, st.staging)
-                idx = st.push(cuda_streams[b])
-                ev = torch.cuda.Event()
-                ev.record(cuda_streams[b])
-                inflight[b].append((ev, k, idx, ta, tn, drop))
+                staging[b] = (pool.submit(stage_and_push, b, k, drop), k, ta, tn, drop)
                 next_k[b] = k + 1
 
         def poll():
@@ -362,21 +392,24 @@ class Server:
                     finish(b)
                 dispatch(b)
 
-        for ta, b, k, tn, drop in arrivals:
-            while now() < ta:
+        try:
+            for ta, b, k, tn, drop in arrivals:
+                while now() < ta:
+                    poll()
+                    time.sleep(0.0002)
+                if ta > tn:
+                    report.late.append((b, k))
+                pending[b][k] = (ta, tn, drop)
+                poll()
+            while any(inflight) or any(pending) or any(x is not None for x in staging):
+                if (not any(inflight) and all(x is None for x in staging) and
+                        all(next_k[b] not in pending[b] for b in range(n) if pending[b])):
+                    raise ValueError("schedule has a gap: batches "
+                                     f"{[(b, sorted(p)) for b, p in enumerate(pending) if p]} "
+                                     "wait for batches that never arrive")
                 poll()
                 time.sleep(0.0002)
-            if ta > tn:
-                report.late.append((b, k))
-            pending[b][k] = (ta, tn, drop)
-            poll()
-        while any(inflight) or any(pending):
-            if not any(inflight) and all(next_k[b] not in pending[b] for b in range(n)
-                                         if pending[b]):
-                raise ValueError("schedule has a gap: batches "
-                                 f"{[(b, sorted(p)) for b, p in enumerate(pending) if p]} "
-                                 "wait for batches that never arrive")
-            poll()
-            time.sleep(0.0002)
+        finally:
+            pool.shutdown(wait=True)
         report.wall = (time.perf_counter() - t0)
         return report
