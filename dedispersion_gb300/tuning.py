@@ -22,6 +22,7 @@ cost model that times only its top candidates.
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import math
 import sys
@@ -174,10 +175,13 @@ def study_shapes(count: int = 400, seed: int = 4242) -> list[Shape]:
     return out
 
 
-def measured_observation(s: Shape, padding: int, max_dms: int = 256, max_samples: int = 8192):
+def measured_observation(s: Shape, padding: int, max_dms: int = 1024,
+                         max_samples: int = 16384):
     """The shape's observation cut to at most max_dms DM trials (per step) and
     max_samples samples, keeping channels, DM step and input width: the
-    per-DM-sample cost of a tile depends on those, not on the trial count."""
+    per-DM-sample cost of a tile depends on those and on how the tiles fill
+    the GPU's waves (a feature of its own), not on the trial count as such.
+    The cut keeps several waves of tiles for most configurations."""
     S = min(s.samples, max_samples)
     bw = 300.0 / s.channels
     if s.subbands:
@@ -192,8 +196,24 @@ def measured_observation(s: Shape, padding: int, max_dms: int = 256, max_samples
 FEATURE_NAMES = ("log2 channels", "log2 rows", "log2 dms", "log2 samples", "log2 subbands+1",
                  "log2 spread", "log2 sharing", "log2 items d0", "log2 items d1",
                  "log2 warps d1", "log2 unroll", "log2 tile dms", "log2 tile samples",
-                 "subband") + tuple(f"bits {b}" for b in BITS) + \
+                 "subband", "log2 waves", "wave efficiency") + \
+    tuple(f"bits {b}" for b in BITS) + \
     tuple(f"variant {v}" for v in VARIANTS) + tuple(f"family {f}" for f in FAMILIES)
+
+
+GPU_SMS = 152  # SMs of a GB300
+
+
+def resident_ctas(name: str, conf: DedispersionConf) -> int:
+    """CTAs of a configuration resident per SM, as its kernel's launch bounds
+    budget them (dd_kernels.cuh): the shared tile one, the others one to four
+    by warps per CTA."""
+    warps = conf.nrThreadsD1
+    if name.startswith("shared8"):
+        return 1
+    if name.startswith("swar8"):
+        return 1 if warps >= 16 else (2 if warps >= 8 else 4)
+    return 2 if warps >= 8 else 4
 
 
 def features(s: Shape, conf: DedispersionConf, name: str) -> np.ndarray:
@@ -205,12 +225,18 @@ def features(s: Shape, conf: DedispersionConf, name: str) -> np.ndarray:
     # Relative-delay growth across eight adjacent rows over the tile's DMs:
     # how often rows share a delay vector (the shared-partial-sum family's gain).
     share = shift0 * s.dm_step * (32 if s.subbands else 1) * tile_d * 8 / max(1, rows)
+    # Waves of tiles on the GPU: tiles / (SMs x resident CTAs per SM), and
+    # how full the last wave is.
+    tile_t = 32 * conf.nrItemsD0
+    dm_count = max(1, s.dms // 32) if s.subbands else max(1, s.dms)
+    tiles = (max(1, s.subbands) * -(-max(1, s.samples) // tile_t) * -(-dm_count // tile_d))
+    waves = tiles / (GPU_SMS * resident_ctas(name, conf))
     f = [math.log2(s.channels), math.log2(rows), math.log2(max(1, s.dms)),
          math.log2(max(1, s.samples)), math.log2(s.subbands + 1), math.log2(1 + spread),
          math.log2(1 + share),
          math.log2(conf.nrItemsD0), math.log2(conf.nrItemsD1), math.log2(conf.nrThreadsD1),
-         math.log2(conf.unroll), math.log2(tile_d), math.log2(32 * conf.nrItemsD0),
-         float(s.subbands > 0)]
+         math.log2(conf.unroll), math.log2(tile_d), math.log2(tile_t),
+         float(s.subbands > 0), math.log2(1 + waves), waves / math.ceil(waves)]
     f += [float(s.bits == b) for b in BITS]
     f += [float(name.endswith("_vkUnpack" + v)) for v in VARIANTS]
     f += [float(name.startswith(fam)) for fam in FAMILIES]
@@ -252,7 +278,11 @@ def collect(shapes: list[Shape], padding: int = 128, iterations: int = 3, device
                     iterations=iterations, device=device)
         units = (obs.getNrDMs(True) * obs.getNrSubbands() * obs.getNrSamplesPerBatch(True)
                  if s.subbands else obs.getNrDMs() * obs.getNrSamplesPerBatch())
-        records.append(StudyRecord(s, res, units))
+        # the record describes the problem that was timed
+        timed = dataclasses.replace(
+            s, dms=obs.getNrDMs(True) * 32 if s.subbands else obs.getNrDMs(),
+            samples=obs.getNrSamplesPerBatch())
+        records.append(StudyRecord(timed, res, units))
         if log and (i % 20 == 0):
             log(f"shape {i}/{len(shapes)}: {s} best {res[0].name} {res[0].mean_ms:.3f} ms")
     return records
@@ -346,6 +376,7 @@ def evaluate(records, tuner: LearnedTuner, test_idx, k: int = 2, seed: int = 7) 
     rng = np.random.default_rng(seed)
     model_r, random_r, default_r, within5 = [], [], [], 0
     t_exhaustive = t_learned = 0.0
+    per_shape = []
     for i in test_idx:
         rec = records[i]
         by_index = {r.kernel: r for r in rec.results}
@@ -355,6 +386,9 @@ def evaluate(records, tuner: LearnedTuner, test_idx, k: int = 2, seed: int = 7) 
         ranked = tuner.rank(rec.shape, cands)[:k]
         infer = time.perf_counter() - t0
         chosen = min(by_index[c.index].mean_ms for c in ranked)
+        per_shape.append({"best": rec.results[0].name, "best_ms": best,
+                          "chosen": [c.name for c in ranked], "chosen_ms": chosen,
+                          "ratio": best / chosen})
         model_r.append(best / chosen)
         within5 += best / chosen >= 0.95
         rnd = rng.choice(len(cands), size=min(k, len(cands)), replace=False)
@@ -370,7 +404,8 @@ def evaluate(records, tuner: LearnedTuner, test_idx, k: int = 2, seed: int = 7) 
             "random_k_vs_best_mean": float(np.mean(random_r)),
             "default_vs_best_mean": float(np.mean(default_r)),
             "tuning_time_exhaustive_s": t_exhaustive, "tuning_time_learned_s": t_learned,
-            "tuning_time_ratio": t_learned / t_exhaustive if t_exhaustive else None}
+            "tuning_time_ratio": t_learned / t_exhaustive if t_exhaustive else None,
+            "per_shape": per_shape}
 
 
 def study(count: int = 400, train_fraction: float = 0.8, steps: int = 3000, k: int = 2,
@@ -412,14 +447,18 @@ def direct_sum_adds(s: Shape) -> float:
 
 
 def bench_report(count: int = 400, k: int = 2, steps: int = 3000, device: int = 0,
-                 full_shapes: int = 2, max_full_adds: float = 2e11) -> dict:
+                 full_shapes: int = 2, max_full_adds: float = 2e11, large_train: int = 120,
+                 max_large_adds: float = 4e11) -> dict:
     """The learned tuner measured for a benchmark line: the study's sweep of
-    `count` seeded shapes (cut to <= 256 DMs x 8192 samples), the model
+    `count` seeded shapes (cut to <= 1024 DMs x 16384 samples), the model
     trained on 80 % of them, its top-k against the exhaustive best on the
     held-out 20 % (k = 1, 2, 4), and the same at full size on the
     1536-channel x 2048-DM x 24576-sample workload (single step and 32
     subbands) plus `full_shapes` held-out shapes of at most `max_full_adds`
-    direct-sum adds, each swept exhaustively at full size."""
+    direct-sum adds, each swept exhaustively at full size.  `large_train`
+    training shapes are also timed cut only to <= 4096 DMs x 32768 samples
+    (at most `max_large_adds` direct-sum adds), so that the model sees how
+    the configurations rank on large problems too."""
     t0 = time.perf_counter()
     shapes = study_shapes(count)
     records = collect(shapes, device=device)
@@ -427,8 +466,17 @@ def bench_report(count: int = 400, k: int = 2, steps: int = 3000, device: int = 
     perm = np.random.default_rng(1).permutation(len(records))
     n_train = int(round(0.8 * len(records)))
     train_idx, test_idx = perm[:n_train], perm[n_train:]
-    X, y, owner = dataset(records)
-    mask = np.isin(owner, train_idx)
+    t0 = time.perf_counter()
+    large = []
+    for i in train_idx:
+        s = shapes[i]
+        cut = dataclasses.replace(s, dms=min(s.dms, 4096), samples=min(s.samples, 32768))
+        if len(large) < large_train and direct_sum_adds(cut) <= max_large_adds:
+            large.append(cut)
+    large_records = collect(large, device=device, full_size=True)
+    t_large = time.perf_counter() - t0
+    X, y, owner = dataset(records + large_records)
+    mask = np.isin(owner, train_idx) | (owner >= len(records))
     tuner = LearnedTuner(device=device)
     t0 = time.perf_counter()
     tuner.fit(X[mask], y[mask], steps=steps)
@@ -457,12 +505,15 @@ def bench_report(count: int = 400, k: int = 2, steps: int = 3000, device: int = 
                                      for s in full],
                           "by_k": {kk: {key: v for key, v in r.items() if key in keys}
                                    for kk, r in full_rep.items()},
+                          "per_shape_top_k": full_rep[str(k)]["per_shape"],
                           "sweep_s": t_full},
-            "study_shapes": count, "train_rows": int(mask.sum()), "collect_s": t_collect,
+            "study_shapes": count, "large_training_shapes": len(large),
+            "large_collect_s": t_large,
+            "train_rows": int(mask.sum()), "collect_s": t_collect,
             "train_s": t_train,
             "network": "3 x 128 ReLU, bf16 weights, fp32 accumulation, trained by the "
                        "library's CUDA kernels (Adam, full batch)",
-            "what": "held-out shapes are cut to <= 256 DMs x 8192 samples for timing; "
+            "what": "held-out shapes are cut to <= 1024 DMs x 16384 samples for timing; "
                     "full_size shapes are timed whole; tuning time = building and timing the "
                     "chosen configurations plus ranking, against the same for all of them"}
 
