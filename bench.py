@@ -69,6 +69,8 @@ def parse():
                     help="skip the 40-beam batched measurement")
     ap.add_argument("--no-served", action="store_true",
                     help="skip the 12-beam serving measurement")
+    ap.add_argument("--served-only", action="store_true",
+                    help="run only the 12-beam serving measurement and print its object")
     ap.add_argument("--no-tuning", action="store_true",
                     help="skip the learned-tuner measurement (400-shape sweep and training)")
     ap.add_argument("--kernel", default=None,
@@ -749,6 +751,10 @@ def main():
     import torch
     import dedispersion_gb300 as dd
     torch.cuda.set_device(local)
+    if args.served_only:
+        rates = dd.measure_add_rate(local, 2)
+        print(json.dumps(bench_served(local, peak_adds=max(rates.values()))))
+        return
     if args.float_only:
         rates = dd.measure_add_rate(local, 2)
         print(json.dumps(bench_float(torch, local, args.steps,
@@ -830,6 +836,24 @@ def main():
                               "gpu_launches": args.steps * plan.launches()}), flush=True)
         return
 
+    sm_mhz = clocks.get("sm_mhz") or 2070.0
+    formula_adds = SMS * LANES * sm_mhz * 1e6
+    # The add roofline's denominator, measured on this GPU now: the faster of
+    # a float-add and an integer-add stream over every SM (dd_measure_add_rate).
+    with ClockSampler(local) as peak_clk:
+        rates = dd.measure_add_rate(local, 3)
+    peak_clocks = peak_clk.summary()
+    peak_adds = max(rates["fadd_per_s"], rates["iadd_per_s"])
+    hbm_peak = 6784.2
+    try:
+        hbm_peak = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"]
+    except Exception:
+        pass
+    # The served line runs first among the extra lines: its latencies are
+    # host-driven, and later lines leave large pinned host arrays and many
+    # plans behind.
+    gc.collect()
+    served = bench_served(local, peak_adds=peak_adds) if not args.no_served else None
     # e2e through the C ABI's synchronous host-buffer call, pinned host memory
     h_in = torch.from_numpy(inp).pin_memory()
     h_out = torch.empty(lay.output_bytes // 4, dtype=torch.float32).pin_memory()
@@ -845,24 +869,7 @@ def main():
     t_e2e = max_over_ranks(time.perf_counter() - t, pg, f"cuda:{local}")
     e2e_value = job_value(world, e2e_steps, D, S, t_e2e)
 
-    sm_mhz = clocks.get("sm_mhz") or 2070.0
-    formula_adds = SMS * LANES * sm_mhz * 1e6
-    # The add roofline's denominator, measured on this GPU now: the faster of
-    # a float-add and an integer-add stream over every SM (dd_measure_add_rate).
-    with ClockSampler(local) as peak_clk:
-        rates = dd.measure_add_rate(local, 3)
-    peak_clocks = peak_clk.summary()
-    peak_adds = max(rates["fadd_per_s"], rates["iadd_per_s"])
-    hbm_peak = 6784.2
-    try:
-        hbm_peak = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"]
-    except Exception:
-        pass
     detect = bench_detect(torch, plan, d_in, d_out, stream, D, S, args.steps)
-    # The served line runs before the lines that leave large host arrays and
-    # many plans behind: its latencies are host-driven.
-    gc.collect()
-    served = bench_served(local, peak_adds=peak_adds) if not args.no_served else None
     ingest_line = bench_ingest(torch, inp, lay, obs, stream)
     subband = bench_subband(torch, local, max(10, min(args.steps, 50)), hbm_peak, peak_adds)
     float32 = bench_float(torch, local, max(3, min(args.steps, 10)), peak_adds, args.float_kernel)

@@ -181,9 +181,11 @@ const dd::KernelInfo *find_kernel(dd_mode mode, uint32_t bits, const dd_conf &c)
     if (c.threads_d0 != 32u || c.threads_d1 != (uint32_t)k.warps_d) continue;
     if (c.items_d0 != (uint32_t)k.items_t || c.items_d1 != (uint32_t)k.items_d) continue;
     if (c.unroll != (uint32_t)k.channels) continue;
-    // items_d2 = rows per shared partial sum marks the shared family.
+    // items_d2 = rows per shared partial sum marks the shared family, 2 the
+    // short-group swar8 tiles.
     const bool shared = c.items_d2 == (uint32_t)dd::kSharedRows;
     if (shared != (k.family == dd::kFamilyShared8)) continue;
+    if ((c.items_d2 == 2u) != (k.max_rows != 0)) continue;
     if (shared && mode != DD_SINGLE_STEP) continue;
     return &k;
   }
@@ -197,9 +199,11 @@ const dd::KernelInfo *find_kernel(dd_mode mode, uint32_t bits, const dd_conf &c)
 // Default tiles of the subband steps, where they differ from the first entry
 // of their input width (fastest of a sweep of every registry entry at 1536
 // channels, 32 subbands, 64 x 32 DMs, 24576 samples: step one's 64 coarse
-// DMs favour 8 DMs per thread, step two's 32 subband rows 8 x 8 items).
+// DMs favour 8 DMs per thread and, with 48 rows per subband, the short-group
+// tile; step two's 32 subband rows 8 x 8 items).  A step-one shape whose
+// subbands have more than 257 rows falls back to the other direct tiles.
 const char *subband_default_name(dd_mode mode, uint32_t fb) {
-  if (mode == DD_STEP_ONE && fb == 8) return "swar8_i2_d8_w8_c16_vkUnpackPermuteMad";
+  if (mode == DD_STEP_ONE && fb == 8) return "swar8s_i4_d8_w8_c8_vkUnpackPermuteMad";
   if (mode == DD_STEP_TWO) return "scalar32_i8_d8_w4_c16";
   return nullptr;
 }
@@ -224,7 +228,7 @@ dd_conf conf_of(const dd::KernelInfo &k) {
   c.split_batches = 0; c.local_mem = 1; c.unroll = k.channels;
   c.threads_d0 = 32; c.threads_d1 = k.warps_d; c.threads_d2 = 1;
   c.items_d0 = k.items_t; c.items_d1 = k.items_d;
-  c.items_d2 = k.family == dd::kFamilyShared8 ? dd::kSharedRows : 1;
+  c.items_d2 = k.family == dd::kFamilyShared8 ? dd::kSharedRows : (k.max_rows ? 2 : 1);
   return c;
 }
 
@@ -431,6 +435,11 @@ dd_status rebuild(dd_plan *p) {
                                    p->device), "query shared memory");
   }
   const bool shared = k.family == dd::kFamilyShared8;
+  if (k.max_rows)
+    for (const dd::GroupDesc &G : p->groups)
+      if (G.entry_count > (uint32_t)k.max_rows)
+        return fail(DD_ERR_UNSUPPORTED, "tile %s takes groups of at most %d rows (a group has %u)",
+                    k.name, k.max_rows, G.entry_count);
   if (p->packed && p->mode == DD_STEP_ONE) {
     if (k.family != dd::kFamilySwar8 || k.items_d % 2)
       return fail(DD_ERR_UNSUPPORTED, "a packed step one runs a swar8 tile (got %s)", k.name);

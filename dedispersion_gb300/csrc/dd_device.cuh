@@ -405,7 +405,10 @@ __device__ __forceinline__ uint32_t mad_lo(uint32_t a, uint32_t b, uint32_t c) {
 
 // Computes one tile; returns false if the CTA must stop (timeout).  `sc`
 // counts the CTA's stages across tiles (mbarrier phase bookkeeping).
-template <int NW, int NDT, int TY, int CH, int VAR>
+// SHORT: every group has at most 257 rows (the host checks), so the 16-bit
+// lanes never pass 2^16 - 1 (257 * 255 = 65535) and need no 32-bit totals:
+// the registers those would take hold more samples per thread instead.
+template <int NW, int NDT, int TY, int CH, int VAR, bool SHORT = false>
 __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
                                            const GroupDesc &G, uint32_t dtile,
                                            uint32_t ttile, uint8_t *smem,
@@ -414,6 +417,7 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
   constexpr int kTileD = TY * NDT;
   constexpr int kThreads = 32 * TY;
   static_assert(CH <= 32 && CH % 2 == 0, "CH rows per stage, even, <= 32");
+  static_assert(!SHORT || VAR != kUnpackMaskHigh, "short groups read lanes (b0, b1), (b2, b3)");
   const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
   const uint32_t t0 = ttile * kTileT, d0 = dtile * kTileD;
   const uint32_t K = G.entry_count;
@@ -442,39 +446,54 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
 
   // kUnpackPermute: lo = (b0, b1) lanes, hi = (b2, b3) lanes.
   // kUnpackMaskHigh: lo = E (b0, b2 lanes), hi = A (w >> 8 sum).
-  uint32_t lo[NDT][NW], hi[NDT][NW], tot[NDT][NW][4];
+  constexpr int TJ = SHORT ? 1 : NDT, TI = SHORT ? 1 : NW;
+  uint32_t lo[NDT][NW], hi[NDT][NW], tot[TJ][TI][4];
 #pragma unroll
   for (int j = 0; j < NDT; ++j)
 #pragma unroll
-    for (int i = 0; i < NW; ++i) {
-      lo[j][i] = hi[j][i] = 0;
+    for (int i = 0; i < NW; ++i) lo[j][i] = hi[j][i] = 0;
+#pragma unroll
+  for (int j = 0; j < TJ; ++j)
+#pragma unroll
+    for (int i = 0; i < TI; ++i)
       tot[j][i][0] = tot[j][i][1] = tot[j][i][2] = tot[j][i][3] = 0;
+  // Sample k (0..3) of word i of DM j: from the totals, or for short groups
+  // straight from the 16-bit lanes.
+  auto lane = [&](int j, int i, int k) -> uint32_t {
+    if constexpr (SHORT) {
+      const uint32_t v = k < 2 ? lo[j][i] : hi[j][i];
+      return (k & 1) ? v >> 16 : v & 0xFFFFu;
+    } else {
+      return tot[j][i][k];
     }
+  };
   uint32_t since = 0;
   using Delays = StageDelays<CH, kTileD, kThreads>;
   Delays delays;
   if (nst) delays.load(P, G, 0, dtile, K < (uint32_t)CH ? K : CH);
 
   auto flush = [&]() {
+    if constexpr (!SHORT) {
 #pragma unroll
-    for (int j = 0; j < NDT; ++j)
+      for (int j = 0; j < NDT; ++j)
 #pragma unroll
-      for (int i = 0; i < NW; ++i) {
-        if (VAR != kUnpackMaskHigh) {
-          tot[j][i][0] += lo[j][i] & 0xFFFFu;
-          tot[j][i][1] += lo[j][i] >> 16;
-          tot[j][i][2] += hi[j][i] & 0xFFFFu;
-          tot[j][i][3] += hi[j][i] >> 16;
-        } else {
-          const uint32_t s2 = lo[j][i] >> 16;
-          const uint32_t x = hi[j][i] - (s2 << 8);
-          tot[j][i][0] += lo[j][i] & 0xFFFFu;
-          tot[j][i][1] += x & 0xFFFFu;
-          tot[j][i][2] += s2;
-          tot[j][i][3] += x >> 16;
+        for (int i = 0; i < NW; ++i) {
+          if (VAR != kUnpackMaskHigh) {
+            tot[j][i][0] += lo[j][i] & 0xFFFFu;
+            tot[j][i][1] += lo[j][i] >> 16;
+            tot[j][i][2] += hi[j][i] & 0xFFFFu;
+            tot[j][i][3] += hi[j][i] >> 16;
+          } else {
+            const uint32_t s2 = lo[j][i] >> 16;
+            const uint32_t x = hi[j][i] - (s2 << 8);
+            tot[j][i][0] += lo[j][i] & 0xFFFFu;
+            tot[j][i][1] += x & 0xFFFFu;
+            tot[j][i][2] += s2;
+            tot[j][i][3] += x >> 16;
+          }
+          lo[j][i] = hi[j][i] = 0;
         }
-        lo[j][i] = hi[j][i] = 0;
-      }
+    }
   };
 
   for (uint32_t s = 0; s < nst; ++s) {
@@ -616,7 +635,7 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
 #pragma unroll
         for (int k = 0; k < 4; ++k)
           w[k] = t + k < P.nr_samples
-                     ? (tot[j][i][k] | (hi_ok ? tot[j + 1][i][k] << 16 : 0u)) : 0u;
+                     ? (lane(j, i, k) | (hi_ok ? lane(j + 1, i, k) << 16 : 0u)) : 0u;
         if (P.out_vec4 && t + 3u < P.nr_samples) {
           *reinterpret_cast<uint4 *>(orow + t) = make_uint4(w[0], w[1], w[2], w[3]);
         } else {
@@ -636,8 +655,8 @@ __device__ __forceinline__ bool swar8_tile(const ProblemDesc &P,
     float *orow = P.out + G.out_offset + (uint64_t)d * P.out_dm_stride;
 #pragma unroll
     for (int i = 0; i < NW; ++i) {
-      const uint32_t v0 = tot[j][i][0], v1 = tot[j][i][1];
-      const uint32_t v2 = tot[j][i][2], v3 = tot[j][i][3];
+      const uint32_t v0 = lane(j, i, 0), v1 = lane(j, i, 1);
+      const uint32_t v2 = lane(j, i, 2), v3 = lane(j, i, 3);
       const uint32_t t = t0 + 4u * (tx + 32u * i);
       if (P.out_vec4 && t + 3u < P.nr_samples) {
         *reinterpret_cast<float4 *>(orow + t) =

@@ -152,6 +152,7 @@ struct KernelInfo {
   const void *func;
   void (*launch)(const ProblemDesc &, unsigned grid, size_t smem,
                  cudaStream_t stream);
+  int max_rows;     // rows a group may have (0: any)
 };
 
 enum { kFamilySwar8 = 0, kFamilyScalar = 1, kFamilyShared8 = 2, kFamilyPair16 = 3 };

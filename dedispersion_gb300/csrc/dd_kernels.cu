@@ -19,7 +19,7 @@ const KernelInfo *kernel_registry(int *count) {
   static std::once_flag once;
   std::call_once(once, [] {
     for (auto part : {kernels_swar8_a, kernels_swar8_b, kernels_swar8_c, kernels_scalar,
-                      kernels_shared8}) {
+                      kernels_shared8, kernels_swar8_s}) {
       int n = 0;
       const KernelInfo *k = part(&n);
       all.insert(all.end(), k, k + n);

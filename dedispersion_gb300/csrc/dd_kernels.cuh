@@ -11,7 +11,7 @@ namespace dd {
 
 
 // Grid-mapped kernel: one CTA per tile.
-template <int NW, int NDT, int TY, int CH, int VAR>
+template <int NW, int NDT, int TY, int CH, int VAR, bool SHORT = false>
 __global__ void __launch_bounds__(32 * TY, (TY >= 16 ? 1 : (TY >= 8 ? 2 : 4)))
     swar8_kernel(const ProblemDesc P) {
   extern __shared__ __align__(128) uint8_t smem[];
@@ -20,7 +20,7 @@ __global__ void __launch_bounds__(32 * TY, (TY >= 16 ? 1 : (TY >= 8 ? 2 : 4)))
   init_barriers(smem, L, CH);
   uint32_t g, dtile, ttile, sc = 0;
   decode_tile(P, blockIdx.x, g, dtile, ttile);
-  (void)swar8_tile<NW, NDT, TY, CH, VAR>(P, P.groups[g], dtile, ttile, smem, L, sc);
+  (void)swar8_tile<NW, NDT, TY, CH, VAR, SHORT>(P, P.groups[g], dtile, ttile, smem, L, sc);
 }
 
 template <typename T, int NS, int NDT, int TY, int CH>
@@ -68,10 +68,10 @@ __global__ void __launch_bounds__(32 * TY, (TY >= 16 ? 1 : 2))
   (void)shared8_tile<NW, ND, TY>(P, g, P.groups[g], dtile, ttile, smem, L, sc);
 }
 
-template <int NW, int NDT, int TY, int CH, int VAR>
+template <int NW, int NDT, int TY, int CH, int VAR, bool SHORT = false>
 void launch_swar8(const ProblemDesc &P, unsigned grid, size_t smem,
                   cudaStream_t stream) {
-  swar8_kernel<NW, NDT, TY, CH, VAR><<<grid, 32 * TY, smem, stream>>>(P);
+  swar8_kernel<NW, NDT, TY, CH, VAR, SHORT><<<grid, 32 * TY, smem, stream>>>(P);
 }
 
 template <typename T, int NS, int NDT, int TY, int CH>
@@ -96,6 +96,14 @@ void launch_shared8(const ProblemDesc &P, unsigned grid, size_t smem,
    4 * NW, NDT, TY, CH, 32 * TY, 128 * NW, TY * NDT, VAR,                    \
    reinterpret_cast<const void *>(&swar8_kernel<NW, NDT, TY, CH, VAR>),      \
    &launch_swar8<NW, NDT, TY, CH, VAR>}
+
+// Short-group swar8 tiles: groups of at most 257 rows only (max_rows; step
+// one's subbands), 16-bit lanes without 32-bit totals (257 * 255 < 2^16).
+#define DD_SWAR8_SHORT(NW, NDT, TY, CH, VAR)                                  \
+  {"swar8s_i" #NW "_d" #NDT "_w" #TY "_c" #CH "_v" #VAR, kFamilySwar8, 8,    \
+   4 * NW, NDT, TY, CH, 32 * TY, 128 * NW, TY * NDT, VAR,                    \
+   reinterpret_cast<const void *>(&swar8_kernel<NW, NDT, TY, CH, VAR, true>), \
+   &launch_swar8<NW, NDT, TY, CH, VAR, true>, 257}
 
 #define DD_SCALAR(T, BITS, NS, NDT, TY, CH)                                   \
   {"scalar" #BITS "_i" #NS "_d" #NDT "_w" #TY "_c" #CH, kFamilyScalar, BITS, \
@@ -130,5 +138,6 @@ const KernelInfo *kernels_swar8_b(int *count);
 const KernelInfo *kernels_swar8_c(int *count);
 const KernelInfo *kernels_scalar(int *count);
 const KernelInfo *kernels_shared8(int *count);
+const KernelInfo *kernels_swar8_s(int *count);
 
 }  // namespace dd

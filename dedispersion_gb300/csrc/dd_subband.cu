@@ -71,7 +71,18 @@ bool subband_try_pack(dd_plan *one, dd_plan *two, const dd_observation *o, const
   const uint32_t flush = (uint32_t)std::max<uint64_t>(1, big ? 0xFFFFu / big : 0xFFFFu);
   int n = 0;
   const KernelInfo *pk = pair_kernels(&n);
-  plan_set_packed(one, nullptr, 0);
+  // The default step-one tile (short groups) takes subbands of at most 257
+  // rows; sub-byte input packs wider subbands, which take the tile with
+  // 32-bit totals instead.
+  const KernelInfo *k1 = nullptr;
+  const uint64_t rows = big / ((1ull << bits) - 1ull);
+  if (rows > 257) {
+    int nk = 0;
+    const KernelInfo *reg = kernel_registry(&nk);
+    for (int i = 0; i < nk && !k1; i++)
+      if (std::strcmp(reg[i].name, "swar8_i2_d8_w8_c16_vkUnpackPermuteMad") == 0) k1 = &reg[i];
+  }
+  plan_set_packed(one, k1, 0);
   plan_set_packed(two, &pk[std::min(std::max(pair_kernel, 0), n - 1)], flush);
   if (plan_ready(one) && plan_ready(two)) return true;
   plan_clear_packed(one);

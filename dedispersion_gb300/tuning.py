@@ -196,7 +196,7 @@ def measured_observation(s: Shape, padding: int, max_dms: int = 1024,
 FEATURE_NAMES = ("log2 channels", "log2 rows", "log2 dms", "log2 samples", "log2 subbands+1",
                  "log2 spread", "log2 sharing", "log2 items d0", "log2 items d1",
                  "log2 warps d1", "log2 unroll", "log2 tile dms", "log2 tile samples",
-                 "subband", "log2 waves", "wave efficiency") + \
+                 "subband", "log2 waves", "wave efficiency", "short groups") + \
     tuple(f"bits {b}" for b in BITS) + \
     tuple(f"variant {v}" for v in VARIANTS) + tuple(f"family {f}" for f in FAMILIES)
 
@@ -236,7 +236,8 @@ def features(s: Shape, conf: DedispersionConf, name: str) -> np.ndarray:
          math.log2(1 + share),
          math.log2(conf.nrItemsD0), math.log2(conf.nrItemsD1), math.log2(conf.nrThreadsD1),
          math.log2(conf.unroll), math.log2(tile_d), math.log2(tile_t),
-         float(s.subbands > 0), math.log2(1 + waves), waves / math.ceil(waves)]
+         float(s.subbands > 0), math.log2(1 + waves), waves / math.ceil(waves),
+         float(name.startswith("swar8s"))]
     f += [float(s.bits == b) for b in BITS]
     f += [float(name.endswith("_vkUnpack" + v)) for v in VARIANTS]
     f += [float(name.startswith(fam)) for fam in FAMILIES]

@@ -130,3 +130,37 @@ def test_zero_dms_is_empty_work(gpu):
     p.run(d_in, 0)
     p.check()
     p.close()
+
+
+def test_every_direct_tile_in_step_one_matches_oracle(gpu, oracle):
+    """Step one through every 1/2/4/8-bit direct configuration, the
+    short-group tiles (groups of at most 257 rows, no 32-bit totals)
+    included; and the short-group tiles refuse groups of more rows."""
+    torch = pytest.importorskip("torch")
+    case = step_one_case(bits=8, padding=64, seed=19, beams=2, sdisp_multiple=8)
+    want = oracle_run(oracle, case)
+    d_in = torch.from_numpy(case.inp).cuda()
+    ran_short = 0
+    for k in dd.kernels():
+        if k.elem_bits != 8 or k.conf.getNrItemsD2() == 8:
+            continue
+        p = dd.Plan(case.obs, dd.DD_STEP_ONE, 8, 64, kernel=k.index)
+        p.setShifts(case.shifts)
+        p.setZappedChannels(case.zapped)
+        d_out = torch.full((case.out_elems,), -1.0, dtype=torch.float32, device="cuda")
+        p.run(d_in, d_out)
+        p.check()
+        p.close()
+        assert_same(d_out.cpu().numpy(), want, case)
+        ran_short += k.name.startswith("swar8s")
+    assert ran_short >= 1
+    big = single_case(C=300, D=8, S=256, bits=8, padding=64, zap=0.0, seed=5)  # 300 rows
+    short = next(k for k in dd.kernels() if k.name.startswith("swar8s"))
+    p = dd.Plan(big.obs, dd.DD_SINGLE_STEP, 8, 64, kernel=short.index)
+    p.setShifts(big.shifts)
+    p.setZappedChannels(big.zapped)
+    p.setBeamMapping(big.mapping)
+    with pytest.raises(dd.DedispersionError) as e:
+        p.run(torch.from_numpy(big.inp).cuda(), torch.zeros(big.out_elems, device="cuda"))
+    assert "at most 257 rows" in str(e.value)
+    p.close()

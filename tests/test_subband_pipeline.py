@@ -68,6 +68,8 @@ CASES = [
     dict(bits=2, padding=16, D1=5),
     dict(bits=1, padding=0, D1=4),
     dict(bits=8, padding=64, D1=9, C=512, SB=4),    # 128 ch per subband: widen every 2 rows
+    dict(bits=4, padding=64, D1=6, C=600, SB=2, zap=0.0),  # 300 rows per subband: the step-one
+                                                            # tile with 32-bit totals
 ]
 
 
