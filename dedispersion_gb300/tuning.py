@@ -300,25 +300,39 @@ def dataset(records: list[StudyRecord]):
 
 
 class LearnedTuner:
-    """MLP over (shape, configuration) features, trained on measured timings."""
+    """MLP over (shape, configuration) features, trained on measured timings;
+    `members` > 1 trains that many networks from different seeds and
+    averages their predictions (an ensemble ranks more steadily than one
+    network, whose training order on the GPU is not deterministic)."""
 
-    def __init__(self, hidden: int = 128, layers: int = 3, seed: int = 0, device: int = 0):
+    def __init__(self, hidden: int = 128, layers: int = 3, seed: int = 0, device: int = 0,
+                 members: int = 1):
         self.hidden, self.layers, self.seed, self.device = hidden, layers, seed, device
-        self.model = None
+        self.members = members
+        self.models = []
         self.mu = self.sd = None
         self.train_loss = None
+
+    @property
+    def model(self):
+        return self.models[0] if self.models else None
 
     def fit(self, X: np.ndarray, y: np.ndarray, steps: int = 3000, lr: float = 1e-3) -> float:
         from .costmodel import MLP
         self.mu, self.sd = X.mean(axis=0), X.std(axis=0) + 1e-6
         self.ymu, self.ysd = float(y.mean()), float(y.std() + 1e-6)
-        self.model = MLP(X.shape[1], self.hidden, self.layers, self.seed, self.device)
-        self.train_loss = self.model.train((X - self.mu) / self.sd, (y - self.ymu) / self.ysd,
-                                           steps, lr)
+        self.models, losses = [], []
+        for m in range(self.members):
+            net = MLP(X.shape[1], self.hidden, self.layers, self.seed + m, self.device)
+            losses.append(net.train((X - self.mu) / self.sd, (y - self.ymu) / self.ysd,
+                                    steps, lr))
+            self.models.append(net)
+        self.train_loss = float(np.mean(losses))
         return self.train_loss
 
     def predict(self, X: np.ndarray) -> np.ndarray:
-        return self.model.forward((X - self.mu) / self.sd) * self.ysd + self.ymu
+        Xn = (X - self.mu) / self.sd
+        return np.mean([net.forward(Xn) for net in self.models], axis=0) * self.ysd + self.ymu
 
     def rank(self, shape: Shape, candidates) -> list:
         X = np.stack([features(shape, k.conf, k.name) for k in candidates])
@@ -327,8 +341,8 @@ class LearnedTuner:
 
     def save(self, path: str) -> None:
         """Weights and normalisation, to rank new shapes without retraining."""
-        np.savez(path, params=self.model.params(), mu=self.mu, sd=self.sd,
-                 ymu=self.ymu, ysd=self.ysd, hidden=self.hidden, layers=self.layers,
+        np.savez(path, params=np.stack([net.params() for net in self.models]), mu=self.mu,
+                 sd=self.sd, ymu=self.ymu, ysd=self.ysd, hidden=self.hidden, layers=self.layers,
                  features=len(self.mu), feature_names=np.array(FEATURE_NAMES))
 
     @classmethod
@@ -337,11 +351,15 @@ class LearnedTuner:
         z = np.load(path)
         if list(z["feature_names"]) != list(FEATURE_NAMES):
             raise ValueError(f"{path} was trained on other features; retrain it")
-        t = cls(hidden=int(z["hidden"]), layers=int(z["layers"]), device=device)
+        params = np.atleast_2d(z["params"])
+        t = cls(hidden=int(z["hidden"]), layers=int(z["layers"]), device=device,
+                members=len(params))
         t.mu, t.sd = z["mu"], z["sd"]
         t.ymu, t.ysd = float(z["ymu"]), float(z["ysd"])
-        t.model = MLP(int(z["features"]), t.hidden, t.layers, 0, device)
-        t.model.set_params(z["params"])
+        for p in params:
+            net = MLP(int(z["features"]), t.hidden, t.layers, 0, device)
+            net.set_params(p)
+            t.models.append(net)
         return t
 
 
@@ -447,9 +465,9 @@ def direct_sum_adds(s: Shape) -> float:
     return float(s.channels) * s.dms * s.samples
 
 
-def bench_report(count: int = 400, k: int = 2, steps: int = 3000, device: int = 0,
-                 full_shapes: int = 2, max_full_adds: float = 2e11, large_train: int = 120,
-                 max_large_adds: float = 4e11) -> dict:
+def bench_report(count: int = 400, k: int = 2, steps: int = 2000, device: int = 0,
+                 full_shapes: int = 8, max_full_adds: float = 2e11, large_train: int = 120,
+                 max_large_adds: float = 4e11, members: int = 3) -> dict:
     """The learned tuner measured for a benchmark line: the study's sweep of
     `count` seeded shapes (cut to <= 1024 DMs x 16384 samples), the model
     trained on 80 % of them, its top-k against the exhaustive best on the
@@ -478,7 +496,7 @@ def bench_report(count: int = 400, k: int = 2, steps: int = 3000, device: int = 
     t_large = time.perf_counter() - t0
     X, y, owner = dataset(records + large_records)
     mask = np.isin(owner, train_idx) | (owner >= len(records))
-    tuner = LearnedTuner(device=device)
+    tuner = LearnedTuner(device=device, members=members)
     t0 = time.perf_counter()
     tuner.fit(X[mask], y[mask], steps=steps)
     t_train = time.perf_counter() - t0
@@ -512,8 +530,9 @@ def bench_report(count: int = 400, k: int = 2, steps: int = 3000, device: int = 
             "large_collect_s": t_large,
             "train_rows": int(mask.sum()), "collect_s": t_collect,
             "train_s": t_train,
-            "network": "3 x 128 ReLU, bf16 weights, fp32 accumulation, trained by the "
-                       "library's CUDA kernels (Adam, full batch)",
+            "network": f"{members} x (3 x 128 ReLU, bf16 weights, fp32 accumulation), "
+                       "trained by the library's CUDA kernels (Adam, full batch), "
+                       "predictions averaged",
             "what": "held-out shapes are cut to <= 1024 DMs x 16384 samples for timing; "
                     "full_size shapes are timed whole; tuning time = building and timing the "
                     "chosen configurations plus ranking, against the same for all of them"}
