@@ -638,7 +638,7 @@ def served_adds(server):
     return total
 
 
-def bench_served(device: int, batches: int = 6, compression: float = 16.0,
+def bench_served(device: int, batches: int = 12, compression: float = 16.0,
                  double_buffer: bool = True, runs: int = 3, peak_adds: float = 0.0):
     """12 beams streaming 2.048 s batches (1536 ch, 25000 samples at 81.92 us,
     8-bit), DM ranges of 1024-4096 DMs at step 0.2, alternating single-step and

@@ -203,17 +203,22 @@ __device__ __forceinline__ uint32_t dev_delay(float first, float step,
 // Sample n lives in byte n / (8 / bits) at bit (n % (8 / bits)) * bits.
 __device__ __forceinline__ uint32_t expand_word(const uint8_t *row, uint32_t k,
                                                 uint32_t bits) {
-  uint32_t v;
-  if (bits == 4)
-    v = reinterpret_cast<const uint16_t *>(row)[k];
-  else if (bits == 2)
-    v = row[k];
-  else
-    v = (row[k >> 1] >> ((k & 1u) * 4u)) & 0xFu;
-  const uint32_t m = (1u << bits) - 1u;
+  if (bits == 4) {
+    // [s1 s0][s3 s2] -> bytes (b0, b0, b1, b1), then the low nibble of
+    // bytes 0 and 2 and the high nibble of bytes 1 and 3.
+    const uint32_t t = __byte_perm(reinterpret_cast<const uint16_t *>(row)[k], 0, 0x1100);
+    return (t & 0x000F000Fu) | ((t >> 4) & 0x0F000F00u);
+  }
+  if (bits == 2) {
+    // Samples 0 and 2 (bits 0-1, 4-5) and 1 and 3 (bits 2-3, 6-7) are moved
+    // into place by two multiplies of disjoint shifted copies (no carries).
+    const uint32_t v = row[k];
+    return (((v & 0x33u) * 0x1001u) & 0x00030003u) | (((v & 0xCCu) * 0x40040u) & 0x03000300u);
+  }
+  const uint32_t v = (row[k >> 1] >> ((k & 1u) * 4u)) & 0xFu;
   uint32_t out = 0;
 #pragma unroll
-  for (int s = 0; s < 4; ++s) out |= ((v >> (s * bits)) & m) << (8 * s);
+  for (int s = 0; s < 4; ++s) out |= ((v >> s) & 1u) << (8 * s);
   return out;
 }
 
