@@ -547,35 +547,21 @@ def bench_subband(torch, device: int, steps: int, hbm_peak: float, peak_adds: fl
                     "HBM; measured (single-pass ncu), step two reads 87 of its 101 MB from DRAM"}
 
 
-def bench_batched(torch, device: int, reps: int = 3, count: int = 40, peak_adds: float = 0.0):
-    """40 uneven beams (384/1536 ch, 8192-32768 samples, 512-4096 DMs, steps
-    0.1-0.5, 2/4/8-bit uniform input) in one CUDA graph launch (the beams'
-    kernels forked over concurrent branches), against the same beams launched
-    one plain kernel each on one stream."""
+def _time_batch(torch, device, beams, kernels, reps):
+    """One batch over `beams` with per-beam configurations `kernels` (None:
+    each beam's default): (ms per batch run, ms per run of the same beams'
+    plain launches one after another with the same configurations, whether
+    every beam's batch output equals its plain output, batch info)."""
     import dedispersion_gb300 as dd
-    from dedispersion_gb300 import synthetic as syn
-    padding = PADDING
-    shapes = syn.batched_shapes(count)
     batch = dd.Batch(device)
-    beams = []
-    units = adds = 0
-    for sh in shapes:
-        obs = syn.shape_observation(sh, padding)
-        shifts = dd.getShifts(obs, padding)
-        zapped = syn.zapped_mask(sh["channels"], 0.05, sh["seed"], padding)
-        mapping = syn.identity_mapping(obs, padding)
-        d_in = syn.device_uniform_input(torch, obs, sh["bits"], padding, sh["seed"])
-        lay = dd.layout(obs, dd.DD_SINGLE_STEP, sh["bits"], padding)
-        d_out = torch.empty(lay.output_bytes // 4, dtype=torch.float32, device=f"cuda:{device}")
-        d_ref = torch.empty_like(d_out)
-        batch.add(obs, sh["bits"], padding, shifts, zapped, mapping, d_in, d_out)
-        plan = dd.Plan(obs, dd.DD_SINGLE_STEP, sh["bits"], padding, device=device)
+    plans = []
+    for (sh, obs, shifts, zapped, mapping, d_in, lay, d_out, d_ref), k in zip(beams, kernels):
+        batch.add(obs, sh["bits"], PADDING, shifts, zapped, mapping, d_in, d_out, kernel=k)
+        plan = dd.Plan(obs, dd.DD_SINGLE_STEP, sh["bits"], PADDING, device=device, kernel=k)
         plan.setShifts(shifts)
         plan.setZappedChannels(zapped)
         plan.setBeamMapping(mapping)
-        beams.append((obs, lay, d_in, d_out, d_ref, plan))
-        units += obs.getNrDMs() * obs.getNrSamplesPerBatch()
-        adds += obs.getNrDMs() * obs.getNrSamplesPerBatch() * int((zapped[:sh["channels"]] == 0).sum())
+        plans.append(plan)
     batch.commit()
     stream = torch.cuda.current_stream()
     batch.run(stream)
@@ -586,33 +572,76 @@ def bench_batched(torch, device: int, reps: int = 3, count: int = 40, peak_adds:
         batch.run(stream)
     e1.record(stream)
     batch.check(stream)
-    t_batch = e0.elapsed_time(e1) / 1e3 / reps
-    for b in beams:
-        b[5].run(b[2], b[4], stream)
+    t_batch = e0.elapsed_time(e1) / reps
+    for b, plan in zip(beams, plans):
+        plan.run(b[5], b[8], stream)
     torch.cuda.synchronize()
     e0.record(stream)
     for _ in range(reps):
-        for b in beams:
-            b[5].run(b[2], b[4], stream)
+        for b, plan in zip(beams, plans):
+            plan.run(b[5], b[8], stream)
     e1.record(stream)
     torch.cuda.synchronize()
-    t_plain = e0.elapsed_time(e1) / 1e3 / reps
+    t_plain = e0.elapsed_time(e1) / reps
     exact = True
-    for obs, lay, d_in, d_out, d_ref, plan in beams:
+    for (sh, obs, shifts, zapped, mapping, d_in, lay, d_out, d_ref), plan in zip(beams, plans):
         S = obs.getNrSamplesPerBatch()
         rows = lay.output_bytes // 4 // lay.output_row_elems
         exact &= bool(torch.equal(d_out.view(rows, -1)[:, :S], d_ref.view(rows, -1)[:, :S]))
         plan.close()
     info = batch.info()
-    shared = info.get("form") == "graph"
     batch.close()
-    return {"value": units / t_batch, "unit": UNIT, "ms_per_batch": t_batch * 1e3,
-            "plain_sequential_value": units / t_plain, "plain_sequential_ms": t_plain * 1e3,
+    return t_batch, t_plain, exact, info
+
+
+def bench_batched(torch, device: int, reps: int = 3, count: int = 40, peak_adds: float = 0.0):
+    """40 uneven beams (384/1536 ch, 8192-32768 samples, 512-4096 DMs, steps
+    0.1-0.5, 2/4/8-bit uniform input) in one CUDA graph launch (the beams'
+    kernels forked over concurrent branches), against the same beams launched
+    one plain kernel each on one stream.  Each beam's configuration is picked
+    by timing a shortlist on it before the batch is recorded
+    (tuning.batch_candidates; outside the timed region); the same batch with
+    each beam's default configuration is reported beside it."""
+    import dedispersion_gb300 as dd
+    from dedispersion_gb300 import synthetic as syn
+    from dedispersion_gb300 import tuning
+    shapes = syn.batched_shapes(count)
+    beams = []
+    units = adds = 0
+    for sh in shapes:
+        obs = syn.shape_observation(sh, PADDING)
+        shifts = dd.getShifts(obs, PADDING)
+        zapped = syn.zapped_mask(sh["channels"], 0.05, sh["seed"], PADDING)
+        mapping = syn.identity_mapping(obs, PADDING)
+        d_in = syn.device_uniform_input(torch, obs, sh["bits"], PADDING, sh["seed"])
+        lay = dd.layout(obs, dd.DD_SINGLE_STEP, sh["bits"], PADDING)
+        d_out = torch.empty(lay.output_bytes // 4, dtype=torch.float32, device=f"cuda:{device}")
+        d_ref = torch.empty_like(d_out)
+        beams.append((sh, obs, shifts, zapped, mapping, d_in, lay, d_out, d_ref))
+        units += obs.getNrDMs() * obs.getNrSamplesPerBatch()
+        adds += obs.getNrDMs() * obs.getNrSamplesPerBatch() * int((zapped[:sh["channels"]] == 0).sum())
+    t0 = time.perf_counter()
+    picks = [tuning.pick(b[1], b[0]["bits"], PADDING, b[2], b[3], b[4], b[5], b[7], device=device)
+             for b in beams]
+    t_tune = time.perf_counter() - t0
+    kernels = [p.kernel for p in picks]
+    t_batch, t_plain, exact, info = _time_batch(torch, device, beams, kernels, reps)
+    d_batch, d_plain, d_exact, _ = _time_batch(torch, device, beams, [None] * len(beams), reps)
+    shared = info.get("form") == "graph"
+    return {"value": units / t_batch * 1e3, "unit": UNIT, "ms_per_batch": t_batch,
+            "plain_sequential_value": units / t_plain * 1e3, "plain_sequential_ms": t_plain,
             "speedup_vs_plain": t_plain / t_batch, "beams": count, "tiles": info["tiles"],
             "adds_per_batch": adds,
-            "adds_frac": adds / t_batch / peak_adds if peak_adds else None,
+            "adds_frac": adds / t_batch * 1e3 / peak_adds if peak_adds else None,
             ("branches" if shared else "persistent_ctas"): info["grid"],
-            "form": info.get("form"), "bit_exact_vs_plain": exact,
+            "form": info.get("form"), "bit_exact_vs_plain": exact and d_exact,
+            "tiles_picked_by": f"timing {len(tuning.batch_candidates())} shortlisted "
+                               f"configurations per beam before recording ({t_tune:.1f} s)",
+            "picked": {name: sum(p.name == name for p in picks)
+                       for name in sorted({p.name for p in picks})},
+            "default_tiles": {"ms_per_batch": d_batch, "value": units / d_batch * 1e3,
+                              "plain_sequential_ms": d_plain,
+                              "adds_frac": adds / d_batch * 1e3 / peak_adds if peak_adds else None},
             "launch": ("one CUDA graph: the beams' kernels on concurrent branches" if shared
                        else "one persistent kernel replayed from a CUDA graph"),
             "workload": "40 beams: 384/1536 ch, 8192-32768 samples, 512-4096 DMs, DM step "

@@ -503,14 +503,17 @@ class Batch:
         self._keep = []
 
     def add(self, observation: Observation, inputBits: int, padding: int, shifts, zapped,
-            mapping, d_input, d_output) -> int:
+            mapping, d_input, d_output, kernel: int | None = None) -> int:
+        """Add one problem; `kernel` (a registry index) sets its configuration
+        in the graph form (dd_batch_add_with_kernel), else its default."""
         sh = np.ascontiguousarray(shifts, dtype=np.float32)
         z, m = _u32(zapped), _u32(mapping)
         idx = C.c_uint32(0)
-        check(lib().dd_batch_add(self._h, C.byref(observation.c), inputBits, padding,
-                                 _ptr(sh, C.c_float), _ptr(z, C.c_uint32), _ptr(m, C.c_uint32),
-                                 C.c_void_p(_devptr(d_input)), C.c_void_p(_devptr(d_output)),
-                                 C.byref(idx)))
+        check(lib().dd_batch_add_with_kernel(
+            self._h, C.byref(observation.c), inputBits, padding, _ptr(sh, C.c_float),
+            _ptr(z, C.c_uint32), _ptr(m, C.c_uint32), C.c_void_p(_devptr(d_input)),
+            C.c_void_p(_devptr(d_output)), -1 if kernel is None else int(kernel),
+            C.byref(idx)))
         self._keep.append((d_input, d_output))
         return idx.value
 

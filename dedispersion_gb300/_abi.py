@@ -153,6 +153,8 @@ SIGNATURES = {
     "dd_batch_create": (C.c_int, [C.POINTER(_P), C.c_int]),
     "dd_batch_add": (C.c_int, [_P, _OBS, C.c_uint32, C.c_uint32, _F32P, _U32P, _U32P, _P, _P,
                                _U32P]),
+    "dd_batch_add_with_kernel": (C.c_int, [_P, _OBS, C.c_uint32, C.c_uint32, _F32P, _U32P,
+                                           _U32P, _P, _P, C.c_int, _U32P]),
     "dd_batch_commit": (C.c_int, [_P]),
     "dd_batch_run": (C.c_int, [_P, _P, C.c_int]),
     "dd_batch_check": (C.c_int, [_P, _P]),

@@ -281,6 +281,14 @@ dd_status dd_batch_add(dd_batch *b, const dd_observation *obs, uint32_t input_bi
                        uint32_t padding, const float *shifts, const uint32_t *zapped,
                        const uint32_t *beam_mapping, const void *d_input, float *d_output,
                        uint32_t *index) {
+  return dd_batch_add_with_kernel(b, obs, input_bits, padding, shifts, zapped, beam_mapping,
+                                  d_input, d_output, -1, index);
+}
+
+dd_status dd_batch_add_with_kernel(dd_batch *b, const dd_observation *obs, uint32_t input_bits,
+                                   uint32_t padding, const float *shifts, const uint32_t *zapped,
+                                   const uint32_t *beam_mapping, const void *d_input,
+                                   float *d_output, int kernel, uint32_t *index) {
   if (!b || !obs || !shifts || !zapped || !beam_mapping || !d_input || !d_output)
     return fail(DD_ERR_INVALID_ARGUMENT, "NULL argument");
   if (input_bits > 8) return fail(DD_ERR_UNSUPPORTED, "batches take 1/2/4/8-bit input");
@@ -298,10 +306,16 @@ dd_status dd_batch_add(dd_batch *b, const dd_observation *obs, uint32_t input_bi
     dd_plan_destroy(p);
     return st;
   }
-  // The beam's own default plan for the graph form (dd_plan_create without a
-  // configuration).
+  // The beam's plan for the graph form: the configuration the caller chose
+  // (registry index `kernel`, e.g. a tuner's pick), or the beam's own default
+  // (dd_plan_create without a configuration).
   dd_plan *q = nullptr;
-  if (dd_plan_create(&q, obs, DD_SINGLE_STEP, input_bits, padding, nullptr, b->device) == DD_OK) {
+  const dd_status cq =
+      kernel >= 0 ? dd_plan_create_with_kernel(&q, obs, DD_SINGLE_STEP, input_bits, padding,
+                                               kernel, b->device)
+                  : dd_plan_create(&q, obs, DD_SINGLE_STEP, input_bits, padding, nullptr,
+                                   b->device);
+  if (cq == DD_OK) {
     bool good = dd_plan_set_shifts(q, shifts, obs->nr_channels) == DD_OK &&
                 dd_plan_set_zapped(q, zapped, obs->nr_channels) == DD_OK &&
                 dd_plan_set_beam_mapping(q, beam_mapping, (size_t)obs->nr_synthesized_beams *
@@ -311,6 +325,10 @@ dd_status dd_batch_add(dd_batch *b, const dd_observation *obs, uint32_t input_bi
       dd_plan_destroy(q);
       q = nullptr;
     }
+  }
+  if (kernel >= 0 && !q) {
+    dd_plan_destroy(p);
+    return fail(DD_ERR_UNSUPPORTED, "configuration %d cannot run this problem", kernel);
   }
   if (b->committed) release(b);
   if (index) *index = (uint32_t)b->plans.size();

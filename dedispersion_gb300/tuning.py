@@ -130,6 +130,33 @@ def sweep(obs, mode: int, bits: int, padding: int, shifts, zapped=None, mapping=
     return out
 
 
+# Configurations a batch times per beam before it commits: every
+# shared-partial-sum tile and the direct tiles that win on some of the
+# batched workload's beams (wide channels, large DM steps).
+BATCH_SHORTLIST = ("shared8_", "swar8_i4_d4_w8_c16_vkUnpackPermuteMad",
+                   "swar8_i4_d4_w16_c16_vkUnpackPermuteMad",
+                   "swar8_i2_d8_w8_c16_vkUnpackPermuteMad")
+
+
+def batch_candidates():
+    """The shortlist of 1-8-bit single-step configurations a batch tunes over."""
+    return [k for k in kernels() if k.elem_bits == 8 and
+            any(k.name.startswith(n) if n.endswith("_") else k.name == n
+                for n in BATCH_SHORTLIST)]
+
+
+def pick(obs, bits: int, padding: int, shifts, zapped, mapping, d_in, d_out, candidates=None,
+         iterations: int = 3, device: int = 0) -> TuneResult:
+    """The fastest of `candidates` (default: :func:`batch_candidates`) on one
+    single-step problem, timed on its own device buffers."""
+    res = sweep(obs, DD_SINGLE_STEP, bits, padding, shifts, zapped, mapping, d_in, d_out,
+                iterations=iterations, device=device,
+                candidates=candidates if candidates is not None else batch_candidates())
+    if not res:
+        raise ValueError("no candidate configuration runs this problem")
+    return res[0]
+
+
 # ---------------------------------------------------------------------------
 # learned tuning
 

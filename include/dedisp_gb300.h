@@ -468,6 +468,17 @@ dd_status dd_batch_add(dd_batch *batch, const dd_observation *obs,
                        const float *shifts, const uint32_t *zapped,
                        const uint32_t *beam_mapping, const void *d_input,
                        float *d_output, uint32_t *index);
+/* dd_batch_add with the problem's configuration chosen by the caller
+ * (registry index `kernel`, dd_kernel_info; -1: the problem's default), for
+ * the graph form: a tuner's per-problem pick.  A configuration that cannot
+ * run the problem is DD_ERR_UNSUPPORTED and adds nothing.  No counterpart
+ * in the reference, whose tuned configuration applies to one kernel launch
+ * (src/Dedispersion.cpp:20-81). */
+dd_status dd_batch_add_with_kernel(dd_batch *batch, const dd_observation *obs,
+                                   uint32_t input_bits, uint32_t padding, const float *shifts,
+                                   const uint32_t *zapped, const uint32_t *beam_mapping,
+                                   const void *d_input, float *d_output, int kernel,
+                                   uint32_t *index);
 dd_status dd_batch_commit(dd_batch *batch);
 /* Enqueue the batch on `stream`: replay the recorded graph (use_graph = 1)
  * or launch directly. */

@@ -130,3 +130,31 @@ def test_batch_of_many_small_beams(gpu):
     assert batch.info()["problems"] == 200 and batch.info()["form"] == "graph"
     _equals_plain(batch, beams, padding)
     batch.close()
+
+
+def test_batch_with_chosen_configurations(gpu, oracle):
+    """Per-beam configurations chosen by the caller (dd_batch_add_with_kernel:
+    a tuner's picks) give each beam exactly its plain output; a configuration
+    that cannot run a beam is refused and adds nothing."""
+    torch = pytest.importorskip("torch")
+    padding = 64
+    beams = build(torch, padding)
+    names = ["swar8_i4_d4_w16_c16_vkUnpackPermuteMad", "shared8_i8_d2_w16",
+             "swar8_i2_d8_w8_c16_vkUnpackPermuteMad", "shared8_i4_d2_w16",
+             "swar8_i4_d4_w8_c16_vkUnpackPermuteMad"]
+    index = {k.name: k.index for k in dd.kernels()}
+    batch = dd.Batch()
+    for b, name in zip(beams, names):
+        sh, obs, shifts, zapped, mapping, d_in, d_out, lay = b
+        batch.add(obs, sh["bits"], padding, shifts, zapped, mapping, d_in, d_out,
+                  kernel=index[name])
+    batch.commit()
+    assert batch.info()["form"] == "graph"
+    _equals_plain(batch, beams, padding)
+    # a 16-bit tile cannot run an 8-bit beam
+    sh, obs, shifts, zapped, mapping, d_in, d_out, lay = beams[0]
+    with pytest.raises(dd.DedispersionError):
+        batch.add(obs, sh["bits"], padding, shifts, zapped, mapping, d_in, d_out,
+                  kernel=index["scalar16_i8_d4_w8_c16"])
+    assert batch.info()["problems"] == len(beams)
+    batch.close()
