@@ -236,3 +236,37 @@ def test_default_tile_follows_the_sharing_gain(gpu, channels, bandwidth, step, w
     assert (ratio < 0.34) == want_shared, ratio
     assert (confs[0].getNrItemsD2() == 8) == want_shared
     np.testing.assert_array_equal(outs[0].view(np.uint32), outs[1].view(np.uint32))
+
+
+def test_table_change_while_a_run_is_in_flight(gpu, oracle):
+    """A setter called right after a run was enqueued on a non-blocking
+    stream: the next use rebuilds the tables and waits for the device before
+    it uploads them, so the run in flight reads the old tables to the end
+    (its output equals the oracle's for the old mask) and the next run uses
+    the new ones."""
+    torch = pytest.importorskip("torch")
+    case = single_case(C=1024, D=512, S=8192, bits=8, padding=128, zap=0.05, seed=61,
+                       fmin=1220.0, tsamp=81.92e-6, step=0.2)
+    new_zapped = case.zapped.copy()
+    new_zapped[:case.obs.getNrChannels() // 2] = 1          # zap half the band
+    plan = dd.Plan(case.obs, dd.DD_SINGLE_STEP, 8, case.padding)
+    plan.setShifts(case.shifts)
+    plan.setZappedChannels(case.zapped)
+    plan.setBeamMapping(case.mapping)
+    d_in = torch.from_numpy(case.inp).cuda()
+    out1 = torch.zeros(case.out_elems, dtype=torch.float32, device="cuda")
+    out2 = torch.zeros_like(out1)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())  # the input copy and the fills
+    plan.run(d_in, out1, s)                 # in flight ...
+    plan.setZappedChannels(new_zapped)      # ... while the mask changes
+    plan.run(d_in, out2, s)
+    plan.check(s)
+    plan.close()
+    want1 = oracle_run(oracle, case)
+    case2 = single_case(C=1024, D=512, S=8192, bits=8, padding=128, zap=0.05, seed=61,
+                        fmin=1220.0, tsamp=81.92e-6, step=0.2)
+    case2.zapped[:] = new_zapped
+    want2 = oracle_run(oracle, case2)
+    same(out1.cpu().numpy(), want1, case)
+    same(out2.cpu().numpy(), want2, case2)
