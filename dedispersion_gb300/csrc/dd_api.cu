@@ -612,6 +612,36 @@ bool shared_worth_it(const dd_plan *p) {
   return direct <= 0 || shared <= kSharedMaxAddsRatio * direct;
 }
 
+// The default direct tile has 8 warps and budgets two CTAs per SM.  Where a
+// shape's window leaves room for only one (wide DM spreads of 8-bit rows:
+// its staged rows and their four shifted copies grow with the spread), the
+// SM would hold 8 warps; the 16-warp tile of the same samples per thread
+// keeps 16.  Measured on 384-channel 8-bit beams with DM steps of 0.42-0.46:
+// 0.334 against 0.429 ms and 0.997 against 1.525 ms.
+void prefer_occupancy(dd_plan *p) {
+  if (p->kinfo->family != dd::kFamilySwar8 || p->kinfo->warps_d != 8) return;
+  int sm_max = 0;
+  if (cudaDeviceGetAttribute(&sm_max, cudaDevAttrMaxSharedMemoryPerMultiprocessor,
+                             p->device) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return;
+  }
+  if (2 * (p->smem + 1024) <= (size_t)sm_max) return;
+  int n = 0;
+  const dd::KernelInfo *reg = dd::kernel_registry(&n);
+  const dd::KernelInfo *eight = p->kinfo, *wide = nullptr;
+  for (int i = 0; i < n && !wide; i++)
+    if (reg[i].family == dd::kFamilySwar8 && !reg[i].max_rows && reg[i].warps_d == 16 &&
+        reg[i].items_t == eight->items_t && reg[i].items_d == eight->items_d &&
+        reg[i].channels == eight->channels && reg[i].variant == eight->variant)
+      wide = &reg[i];
+  if (!wide) return;
+  p->kinfo = wide;
+  if (rebuild(p) == DD_OK) return;
+  p->kinfo = eight;
+  (void)rebuild(p);
+}
+
 dd_status rebuild_auto(dd_plan *p) {
   if (p->auto_kernel) p->kinfo = default_kernel(p->mode, p->bits, true);
   dd_status st = rebuild(p);
@@ -620,6 +650,7 @@ dd_status rebuild_auto(dd_plan *p) {
     const dd::KernelInfo *shared = p->kinfo;
     p->kinfo = default_kernel(p->mode, p->bits, false);
     st = rebuild(p);
+    if (st == DD_OK && p->mode == DD_SINGLE_STEP) prefer_occupancy(p);
     if (st == DD_OK) return st;
     p->kinfo = shared;  // the direct tile does not fit: keep the shared one
     return rebuild(p);

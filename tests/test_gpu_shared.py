@@ -270,3 +270,24 @@ def test_table_change_while_a_run_is_in_flight(gpu, oracle):
     want2 = oracle_run(oracle, case2)
     same(out1.cpu().numpy(), want1, case)
     same(out2.cpu().numpy(), want2, case2)
+
+
+def test_default_direct_tile_keeps_two_ctas_worth_of_warps(gpu, oracle):
+    """384 channels of 8-bit input at a DM step of 0.46: the shared tile is
+    not worth it, and the 8-warp direct tile's staged window (a wide DM
+    spread) leaves room for one CTA per SM; the default then takes the
+    16-warp tile of the same shape, with the oracle's output."""
+    torch = pytest.importorskip("torch")
+    case = single_case(C=384, D=256, S=4096, bits=8, padding=128, zap=0.05, seed=67,
+                       fmin=1220.0, bw=0.78125, tsamp=81.92e-6, step=0.459)
+    p = dd.Plan(case.obs, dd.DD_SINGLE_STEP, 8, 128)
+    p.setShifts(case.shifts)
+    p.setZappedChannels(case.zapped)
+    p.setBeamMapping(case.mapping)
+    d_out = torch.zeros(case.out_elems, dtype=torch.float32, device="cuda")
+    p.run(torch.from_numpy(case.inp).cuda(), d_out)
+    p.check()
+    conf = p.conf()
+    p.close()
+    assert conf.getNrItemsD2() == 1 and conf.getNrThreadsD1() == 16, conf.print()
+    same(d_out.cpu().numpy(), oracle_run(oracle, case), case)
