@@ -547,7 +547,7 @@ def bench_subband(torch, device: int, steps: int, hbm_peak: float, peak_adds: fl
                     "HBM; measured (single-pass ncu), step two reads 87 of its 101 MB from DRAM"}
 
 
-def _time_batch(torch, device, beams, kernels, reps):
+def _time_batch(torch, device, beams, kernels, reps, persistent=False):
     """One batch over `beams` with per-beam configurations `kernels` (None:
     each beam's default): (ms per batch run, ms per run of the same beams'
     plain launches one after another with the same configurations, whether
@@ -562,6 +562,8 @@ def _time_batch(torch, device, beams, kernels, reps):
         plan.setZappedChannels(zapped)
         plan.setBeamMapping(mapping)
         plans.append(plan)
+    if persistent:
+        batch.setPersistent(True)
     batch.commit()
     stream = torch.cuda.current_stream()
     batch.run(stream)
@@ -627,6 +629,8 @@ def bench_batched(torch, device: int, reps: int = 3, count: int = 40, peak_adds:
     kernels = [p.kernel for p in picks]
     t_batch, t_plain, exact, info = _time_batch(torch, device, beams, kernels, reps)
     d_batch, d_plain, d_exact, _ = _time_batch(torch, device, beams, [None] * len(beams), reps)
+    p_batch, _, p_exact, p_info = _time_batch(torch, device, beams, [None] * len(beams), reps,
+                                              persistent=True)
     shared = info.get("form") == "graph"
     return {"value": units / t_batch * 1e3, "unit": UNIT, "ms_per_batch": t_batch,
             "plain_sequential_value": units / t_plain * 1e3, "plain_sequential_ms": t_plain,
@@ -634,7 +638,7 @@ def bench_batched(torch, device: int, reps: int = 3, count: int = 40, peak_adds:
             "adds_per_batch": adds,
             "adds_frac": adds / t_batch * 1e3 / peak_adds if peak_adds else None,
             ("branches" if shared else "persistent_ctas"): info["grid"],
-            "form": info.get("form"), "bit_exact_vs_plain": exact and d_exact,
+            "form": info.get("form"), "bit_exact_vs_plain": exact and d_exact and p_exact,
             "tiles_picked_by": f"timing {len(tuning.batch_candidates())} shortlisted "
                                f"configurations per beam before recording ({t_tune:.1f} s)",
             "picked": {name: sum(p.name == name for p in picks)
@@ -642,6 +646,11 @@ def bench_batched(torch, device: int, reps: int = 3, count: int = 40, peak_adds:
             "default_tiles": {"ms_per_batch": d_batch, "value": units / d_batch * 1e3,
                               "plain_sequential_ms": d_plain,
                               "adds_frac": adds / d_batch * 1e3 / peak_adds if peak_adds else None},
+            "persistent_form": {"ms_per_batch": p_batch, "value": units / p_batch * 1e3,
+                                "adds_frac": adds / p_batch * 1e3 / peak_adds if peak_adds else None,
+                                "ctas": p_info["grid"],
+                                "what": "one persistent direct-tile kernel over all 40 beams' "
+                                        "tiles, replayed from a CUDA graph"},
             "launch": ("one CUDA graph: the beams' kernels on concurrent branches" if shared
                        else "one persistent kernel replayed from a CUDA graph"),
             "workload": "40 beams: 384/1536 ch, 8192-32768 samples, 512-4096 DMs, DM step "
