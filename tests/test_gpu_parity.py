@@ -164,3 +164,16 @@ def test_every_direct_tile_in_step_one_matches_oracle(gpu, oracle):
         p.run(torch.from_numpy(big.inp).cuda(), torch.zeros(big.out_elems, device="cuda"))
     assert "at most 257 rows" in str(e.value)
     p.close()
+
+
+def test_measured_add_rate_is_plausible(gpu):
+    """dd_measure_add_rate, the roofline's denominator: float and integer add
+    streams over every SM land between a quarter and 1.2x the rate of 128
+    adds per SM clock at the device's maximum clock."""
+    torch = pytest.importorskip("torch")
+    props = torch.cuda.get_device_properties(0)
+    rates = dd.measure_add_rate(0, 2)
+    clock_hz = 2.2e9  # above the GB300's maximum SM clock (2.07 GHz)
+    top = props.multi_processor_count * 128 * clock_hz
+    for name in ("fadd_per_s", "iadd_per_s"):
+        assert 0.25 * top < rates[name] < 1.2 * top, (name, rates[name], top)
