@@ -52,6 +52,26 @@ class _TimeMajorFile:
             return buf.reshape(count, self.nchans)
         return buf
 
+    @property
+    def nsamples(self) -> int:
+        return int(self.info.nsamples)
+
+    def read_into(self, start: int, out: np.ndarray) -> int:
+        """Read time samples from ``start`` into ``out`` (a contiguous 8-bit
+        [count][nchans] array, e.g. a stream's pinned staging): as many as the
+        file holds, the rest of ``out`` zero.  Returns the samples read."""
+        if self.nbits != 8:
+            raise ValueError("read_into takes 8-bit files")
+        if out.dtype != np.uint8 or not out.flags.c_contiguous or out.size % self.nchans:
+            raise ValueError("out must be a contiguous uint8 [count][nchans] array")
+        count = out.size // self.nchans
+        have = max(0, min(count, self.nsamples - int(start)))
+        if have:
+            self._read(int(start), have, C.c_void_p(out.ctypes.data))
+        if have < count:
+            out.reshape(count, self.nchans)[have:] = 0
+        return have
+
     def to_rows(self, d_block, d_rows, row_bytes: int, offset: int = 0, stream=None) -> None:
         """Device: time-major 8-bit block -> channel rows at sample ``offset``."""
         from . import _devptr, _stream

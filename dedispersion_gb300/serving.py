@@ -55,6 +55,8 @@ class BeamConfig:
     zap_fraction: float = 0.05
     seed: int = 0
     double_buffer: bool = False    # two pinned staging/output pairs, two batches in flight
+    time_major: bool = False       # batches arrive as file-order [samples][channels] blocks
+    reverse: bool = False          # (time-major) file channel 0 is the highest frequency
 
     @property
     def period(self) -> float:
@@ -203,6 +205,33 @@ def served_beams(count: int = 12, seed: int = 77, padding: int = 128,
     return out
 
 
+class FileSource:
+    """A `source` for Server.serve that reads each beam's batches straight
+    from its SIGPROC filterbank or PSRDADA file (``ingest.Filterbank`` /
+    ``ingest.Dada``, 8-bit) into the stream's pinned staging: batch k of beam
+    b is samples [k S, (k + 1) S) of its file, past the end zeros.  The
+    beams are admitted with ``time_major`` (and ``reverse`` = the file's
+    channel order), so the file-order block goes to the device as it is and
+    is transposed into the ring there.  With the server's staging pool and
+    double-buffered streams, a beam's next read overlaps the GPU work of its
+    batch in flight: file -> pinned host -> device ring, no other host copy."""
+
+    def __init__(self, files) -> None:
+        self.files = list(files)
+
+    @staticmethod
+    def config(file, name: str, **kw) -> BeamConfig:
+        """A BeamConfig matching a file's channels, band and sampling time."""
+        obs = file.observation(Observation())
+        return BeamConfig(name=name, channels=obs.getNrChannels(), min_freq=obs.getMinFreq(),
+                          bandwidth=obs.getChannelBandwidth(),
+                          sampling_time=obs.getSamplingTime(), time_major=True,
+                          reverse=file.reversed, **kw)
+
+    def __call__(self, b: int, k: int, staging: np.ndarray) -> None:
+        self.files[b].read_into(k * staging.shape[0], staging)
+
+
 def poisson_schedule(beams: int, batches: int, period: float, jitter: float, seed: int):
     """Arrivals (time, beam, batch): batch k of beam b at phase_b + k * period +
     Exp(jitter), sorted by time."""
@@ -272,11 +301,15 @@ class Server:
 
     def admit(self, cfg: BeamConfig) -> Stream:
         need, _ = stream_bytes(cfg)
+        if cfg.time_major:
+            need += cfg.samples * cfg.channels  # the device block transposed into the ring
         if self.used + need > self.budget:
             raise DedispersionError(_abi.DD_ERR_OVER_BUDGET,
                                     f"beam {cfg.name} needs {need} device bytes, "
                                     f"{self.budget - self.used} of the budget are left")
         s = Stream(cfg, self.device)
+        if cfg.time_major:
+            s.set_time_major(cfg.reverse)
         if cfg.double_buffer:
             s.set_double_buffer(True)
         self.used += s.device_bytes

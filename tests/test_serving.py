@@ -255,3 +255,49 @@ def test_late_and_dropped_batches(gpu):
                                       want.view(np.uint32)), (cfg.name, k)
             prev = window[:, window.shape[1] - stream.tail:] if stream.tail else prev
     server.close()
+
+
+@pytest.mark.gpu
+def test_file_source_serves_files(gpu, tmp_path):
+    """Beams served straight from files (serving.FileSource): a SIGPROC
+    filterbank with descending frequencies and a PSRDADA file with ascending
+    ones, three batches each plus a partial fourth, read into the streams'
+    pinned staging and transposed on the device; every batch equals the
+    plain path on its window of the channel rows the files were written
+    from (past the end of a file, zeros)."""
+    pytest.importorskip("torch")
+    from dedispersion_gb300 import ingest
+    C, S, nb = 192, 2048, 4
+    rng = np.random.default_rng(17)
+    rows = [rng.integers(0, 256, size=(C, 3 * S + S // 2), dtype=np.uint8) for _ in range(2)]
+    fil, dada = tmp_path / "beam0.fil", tmp_path / "beam1.dada"
+    ingest.write_filterbank(str(fil), rows[0][::-1].T, fch1=1300.0 + (C - 1) * 0.5, foff=-0.5,
+                            tsamp=81.92e-6)
+    ingest.write_dada(str(dada), rows[1].T, freq=1300.0 - 0.25 + C * 0.5 / 2, bw=C * 0.5,
+                      tsamp_us=81.92)
+    files = [ingest.Filterbank(str(fil)), ingest.Dada(str(dada))]
+    assert files[0].reversed and not files[1].reversed
+    cfgs = [serving.FileSource.config(f, f"file{i}", samples=S, dms=64, dm_step=0.2, seed=i,
+                                      double_buffer=True)
+            for i, f in enumerate(files)]
+    server = serving.Server(budget_bytes=150 * 10**9)
+    for c in cfgs:
+        server.admit(c)
+    outputs = {}
+
+    def consumer(b, k, out):
+        outputs[(b, k)] = out.copy()
+
+    sched = [(0.0, b, k) for k in range(nb) for b in range(2)]
+    report = server.serve(sched, serving.FileSource(files), consumer)
+    assert report.summary()["batches"] == 2 * nb
+    for b, stream in enumerate(server.streams):
+        padded = np.zeros((C, nb * S), np.uint8)
+        padded[:, :rows[b].shape[1]] = rows[b]
+        prev = np.zeros((C, stream.tail), np.uint8)
+        for k in range(nb):
+            window = np.concatenate([prev, padded[:, k * S:(k + 1) * S]], axis=1)
+            want = plain_reference(stream, window)
+            assert np.array_equal(outputs[(b, k)].view(np.uint32), want.view(np.uint32)), (b, k)
+            prev = window[:, window.shape[1] - stream.tail:]
+    server.close()
