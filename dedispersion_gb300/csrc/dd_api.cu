@@ -22,6 +22,7 @@
 #include "dd_internal.h"
 #include "dd_shared.cuh"
 #include "dd_shared_plan.h"
+#include "dd_tmem.cuh"
 
 namespace {
 
@@ -185,8 +186,11 @@ const dd::KernelInfo *find_kernel(dd_mode mode, uint32_t bits, const dd_conf &c)
     // short-group swar8 tiles.
     const bool shared = c.items_d2 == (uint32_t)dd::kSharedRows;
     if (shared != (k.family == dd::kFamilyShared8)) continue;
+    // items_d2 = 3 marks the TMEM-window tile.
+    const bool tmem = c.items_d2 == 3u;
+    if (tmem != (k.family == dd::kFamilyTmem32)) continue;
     if ((c.items_d2 == 2u) != (k.max_rows != 0)) continue;
-    if (shared && mode != DD_SINGLE_STEP) continue;
+    if ((shared || tmem) && mode != DD_SINGLE_STEP) continue;
     return &k;
   }
   return nullptr;
@@ -215,10 +219,14 @@ const dd::KernelInfo *default_kernel(dd_mode mode, uint32_t bits, bool shared) {
   if (const char *name = subband_default_name(mode, fb))
     for (int i = 0; i < n; i++)
       if (std::strcmp(reg[i].name, name) == 0) return &reg[i];
+  // `shared`: the preferred tile of plans without a configuration -- shared
+  // partial sums for 1-8-bit single-step input, TMEM windows for float.
   const bool want_shared = shared && mode == DD_SINGLE_STEP && bits <= 8;
+  const bool want_tmem = shared && mode == DD_SINGLE_STEP && bits == 32;
   for (int i = 0; i < n; i++)
     if ((uint32_t)reg[i].elem_bits == fb &&
-        (reg[i].family == dd::kFamilyShared8) == want_shared)
+        (reg[i].family == dd::kFamilyShared8) == want_shared &&
+        (reg[i].family == dd::kFamilyTmem32) == want_tmem)
       return &reg[i];
   return nullptr;
 }
@@ -228,7 +236,9 @@ dd_conf conf_of(const dd::KernelInfo &k) {
   c.split_batches = 0; c.local_mem = 1; c.unroll = k.channels;
   c.threads_d0 = 32; c.threads_d1 = k.warps_d; c.threads_d2 = 1;
   c.items_d0 = k.items_t; c.items_d1 = k.items_d;
-  c.items_d2 = k.family == dd::kFamilyShared8 ? dd::kSharedRows : (k.max_rows ? 2 : 1);
+  c.items_d2 = k.family == dd::kFamilyShared8  ? dd::kSharedRows
+               : k.family == dd::kFamilyTmem32 ? 3
+                                               : (k.max_rows ? 2 : 1);
   return c;
 }
 
@@ -460,6 +470,23 @@ dd_status rebuild(dd_plan *p) {
   } else if (k.family == dd::kFamilyPair16) {
     return fail(DD_ERR_UNSUPPORTED, "pair tiles read a packed step-one intermediate only");
   }
+  const bool tmem = k.family == dd::kFamilyTmem32;
+  uint32_t rows_max = 0;
+  for (const dd::GroupDesc &G : p->groups) rows_max = std::max(rows_max, G.entry_count);
+  if (tmem) {
+    if (p->mode != DD_SINGLE_STEP || p->bits != 32)
+      return fail(DD_ERR_UNSUPPORTED, "kernel %s computes single-step float input only", k.name);
+    if (dd::tmem_smem_bytes(rows_max) > (size_t)dev_max)
+      return fail(DD_ERR_UNSUPPORTED, "tile %s holds the rows of a group in shared memory "
+                  "(%u rows need %zu bytes, device allows %d)",
+                  k.name, rows_max, dd::tmem_smem_bytes(rows_max), dev_max);
+    if (d.input_bytes / 16 > 0xFFFFFFFFull)
+      return fail(DD_ERR_UNSUPPORTED, "tile %s addresses rows in 16-byte units of 32 bits",
+                  k.name);
+    if (!dd::tmem_fits(uniq.data(), uniq.size(), d.first_dm, d.dm_step, d.nr_dms))
+      return fail(DD_ERR_UNSUPPORTED, "tile %s: 16 DMs spread a row's delay by more than %u "
+                  "samples", k.name, dd::kTmMaxOff - 3u);
+  }
   if (shared) {
     if (p->mode != DD_SINGLE_STEP || p->bits > 8)
       return fail(DD_ERR_UNSUPPORTED, "kernel %s computes single-step 1/2/4/8-bit input only",
@@ -473,7 +500,7 @@ dd_status rebuild(dd_plan *p) {
   }
   const uint32_t bits = family_bits(p->mode, p->bits) == 8 ? p->bits : family_bits(p->mode, p->bits);
   const uint32_t a = dd::window_alignment_samples(bits);
-  p->win = shared ? 0 : ((k.tile_t + spread + a + 8) + 15) / 16 * 16;
+  p->win = shared ? 0 : tmem ? rows_max : ((k.tile_t + spread + a + 8) + 15) / 16 * 16;
   p->smem = shared ? p->shared.smem : dd::kernel_smem_bytes(k, p->win, bits);
   if (p->smem > (size_t)dev_max)
     return fail(DD_ERR_UNSUPPORTED,
@@ -484,7 +511,7 @@ dd_status rebuild(dd_plan *p) {
   // first DM, per delay row (the same float order as the device's
   // dev_delay).  16-bit offsets: skipped if a spread does not fit.
   const size_t rows = p->delay_shift.size();
-  p->use_delay_tables = !shared && spread < 65536 && rows > 0 && p->tiles_d > 0;
+  p->use_delay_tables = !shared && !tmem && spread < 65536 && rows > 0 && p->tiles_d > 0;
   if (p->use_delay_tables) {
     p->delay_rel.assign((size_t)p->tiles_d * rows * k.tile_d, 0);
     // DM values in the reference's order (firstDM + dm * dmStep, each op
@@ -584,8 +611,15 @@ dd_status rebuild(dd_plan *p) {
     if (us) return us;
   }
   // The attribute is a cap shared by every plan of this kernel: set it to the
-  // device maximum so that no plan lowers it below another plan's need.
-  DD_CUDA(cudaFuncSetAttribute(k.func, cudaFuncAttributeMaxDynamicSharedMemorySize, dev_max),
+  // device maximum (less the kernel's static shared memory) so that no plan
+  // lowers it below another plan's need.
+  cudaFuncAttributes fa{};
+  DD_CUDA(cudaFuncGetAttributes(&fa, k.func), "query kernel attributes");
+  if (p->smem + fa.sharedSizeBytes > (size_t)dev_max)
+    return fail(DD_ERR_UNSUPPORTED, "tile %s needs %zu + %zu bytes of shared memory, device "
+                "allows %d", k.name, p->smem, (size_t)fa.sharedSizeBytes, dev_max);
+  DD_CUDA(cudaFuncSetAttribute(k.func, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               dev_max - (int)fa.sharedSizeBytes),
           "set kernel shared memory");
   p->ready = true;
   return DD_OK;
@@ -1134,9 +1168,10 @@ dd_status dd_plan_run(dd_plan *p, const void *d_input, float *d_output, void *st
   DeviceGuard g(p->device);
   if (!g.ok) return fail(DD_ERR_CUDA, "cannot select device %d", p->device);
   p->launched = true;
-  // The shared, swar8 and pair tiles take part (the scalar tile launches as
-  // usual).
-  if (p->overlap && p->kinfo->family != dd::kFamilyScalar) {
+  // The shared, swar8 and pair tiles take part (the scalar and TMEM-window
+  // tiles launch as usual; the latter holds all of an SM's TMEM per CTA).
+  if (p->overlap && p->kinfo->family != dd::kFamilyScalar &&
+      p->kinfo->family != dd::kFamilyTmem32) {
     // A programmatic dependent of the stream's previous kernel: its tiles
     // start on SMs the previous launch's last wave leaves idle.
     P.overlap = 1;

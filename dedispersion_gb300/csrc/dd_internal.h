@@ -80,7 +80,8 @@ struct ProblemDesc {
   uint32_t bits;           // 1, 2, 4, 8, 16 or 32 (float)
   float first_dm;
   float dm_step;
-  uint32_t win_samples;    // samples staged per row and tile
+  uint32_t win_samples;    // samples staged per row and tile (kFamilyTmem32: rows
+                           // per group the shared memory holds)
   uint32_t tiles_t;        // time tiles per group
   uint32_t tiles_d;        // DM tiles per group
   uint32_t tma;            // 1: rows staged by bulk async copies
@@ -139,7 +140,7 @@ struct ProblemDesc {
 // One entry of the kernel registry: a compiled tile configuration.
 struct KernelInfo {
   const char *name;
-  int family;       // kFamilySwar8, kFamilyScalar or kFamilyShared8
+  int family;       // kFamilySwar8, kFamilyScalar, kFamilyShared8, kFamilyPair16, kFamilyTmem32
   int elem_bits;    // swar8: 8 (covers 1/2/4/8); scalar: 16 or 32
   int items_t;      // samples per thread
   int items_d;      // DMs per thread
@@ -155,7 +156,7 @@ struct KernelInfo {
   int max_rows;     // rows a group may have (0: any)
 };
 
-enum { kFamilySwar8 = 0, kFamilyScalar = 1, kFamilyShared8 = 2, kFamilyPair16 = 3 };
+enum { kFamilySwar8 = 0, kFamilyScalar = 1, kFamilyShared8 = 2, kFamilyPair16 = 3, kFamilyTmem32 = 4 };
 
 // Registry of compiled configurations (dd_kernels.cu).
 const KernelInfo *kernel_registry(int *count);

@@ -138,6 +138,7 @@ const KernelInfo *kernels_swar8_b(int *count);
 const KernelInfo *kernels_swar8_c(int *count);
 const KernelInfo *kernels_scalar(int *count);
 const KernelInfo *kernels_shared8(int *count);
+const KernelInfo *kernels_tmem(int *count);
 const KernelInfo *kernels_swar8_s(int *count);
 
 }  // namespace dd

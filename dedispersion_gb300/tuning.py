@@ -55,10 +55,11 @@ class TuneResult:
 
 def family_kernels(mode: int, bits: int):
     """Compiled configurations for a mode and input width; the
-    shared-partial-sum ones (items_d2 = 8) compute single-step input only."""
+    shared-partial-sum ones (items_d2 = 8) and the TMEM-window one
+    (items_d2 = 3) compute single-step input only."""
     fam = 32 if mode == DD_STEP_TWO else (8 if bits <= 8 else bits)
     return [k for k in kernels() if k.elem_bits == fam and
-            (mode == DD_SINGLE_STEP or k.conf.getNrItemsD2() != 8)]
+            (mode == DD_SINGLE_STEP or k.conf.getNrItemsD2() not in (8, 3))]
 
 
 def _time_plan(plan: Plan, d_in, d_out, warmup: int, iterations: int):
@@ -162,7 +163,7 @@ def pick(obs, bits: int, padding: int, shifts, zapped, mapping, d_in, d_out, can
 
 BITS = (2, 4, 8, 32)
 VARIANTS = ("PermuteMad", "Permute", "PermuteHalf", "MaskHigh")  # swar8 name suffixes
-FAMILIES = ("swar8", "scalar", "shared8")                           # name prefixes
+FAMILIES = ("swar8", "scalar", "shared8", "tmem32")                 # name prefixes
 # Delay per unit DM of the lowest channel, in samples, for the study band
 # (1220-1520 MHz at 81.92 us); the window spread of a tile scales with it.
 STUDY_SHIFT0 = 12.1
@@ -233,10 +234,10 @@ GPU_SMS = 152  # SMs of a GB300
 
 def resident_ctas(name: str, conf: DedispersionConf) -> int:
     """CTAs of a configuration resident per SM, as its kernel's launch bounds
-    budget them (dd_kernels.cuh): the shared tile one, the others one to four
-    by warps per CTA."""
+    budget them (dd_kernels.cuh): the shared and TMEM-window tiles one, the
+    others one to four by warps per CTA."""
     warps = conf.nrThreadsD1
-    if name.startswith("shared8"):
+    if name.startswith(("shared8", "tmem32")):
         return 1
     if name.startswith("swar8"):
         return 1 if warps >= 16 else (2 if warps >= 8 else 4)

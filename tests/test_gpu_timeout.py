@@ -9,7 +9,7 @@ on copies that have not landed yet: the run must report DD_ERR_TIMEOUT, and
 the same plan with the default limit restored must then give the oracle's
 output (include/Dedispersion.hpp:70-109), for every kernel family (the
 shared-partial-sum tile, the direct swar8 tile, the scalar tiles for 16-bit
-and float input).  The reference reports OpenCL errors to its caller in the
+and float input, the TMEM-window tile for float input).  The reference reports OpenCL errors to its caller in the
 same way (src/DedispersionTuning.cpp:396-409).
 """
 import numpy as np
@@ -32,6 +32,7 @@ CASES = [
     ("swar8", 8, "swar8_i4_d4_w8_c16_vkUnpackPermuteMad"),
     ("scalar16", 16, "scalar16_i8_d4_w8_c16"),
     ("scalar32", 32, "scalar32_i8_d8_w4_c16"),
+    ("tmem32", 32, "tmem32_t16_d64"),
 ]
 
 
