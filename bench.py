@@ -82,6 +82,9 @@ def parse():
     ap.add_argument("--float-only", action="store_true",
                     help="run only the float32-input line (--steps runs after 2 warm-up runs; "
                          "the command ncu captures for the float kernel)")
+    ap.add_argument("--float-dms", type=int, default=None, metavar="D",
+                    help="with --float-only: the first D of the 2048 DM trials (a smaller case "
+                         "of the same rows for a full ncu capture)")
     ap.add_argument("--float-kernel", default=None,
                     help="registry name of the float tile for the float32 line (default: the "
                          "library's float default)")
@@ -344,14 +347,18 @@ def bench_ingest(torch, inp, lay, obs, stream):
                     "descending-frequency file order reversed on the way"}
 
 
-def bench_float(torch, device: int, steps: int, peak_adds: float, kernel: str | None = None):
+def bench_float(torch, device: int, steps: int, peak_adds: float, kernel: str | None = None,
+                dms: int | None = None):
     """Config 2 with float32 input (N(128, 20), same channels, DMs, zapping):
     throughput of the float path (summed in the reference's channel order),
     and its largest relative error against an FP64 sum of four DM rows
-    computed here with numpy."""
+    computed here with numpy.  `dms` keeps only the first DM trials (the
+    profiling case)."""
     import dedispersion_gb300 as dd
     from dedispersion_gb300 import synthetic as syn
     obs = syn.large_observation(PADDING)
+    if dms:
+        obs.setDMRange(dms, obs.getFirstDM(), obs.getDMStep())
     shifts = dd.getShifts(obs, PADDING)
     zapped = syn.zapped_mask(1536, 0.05, 7, PADDING)
     mapping = syn.identity_mapping(obs, PADDING)
@@ -384,12 +391,12 @@ def bench_float(torch, device: int, steps: int, peak_adds: float, kernel: str | 
     e1.record(stream)
     p.check(stream)
     t = e0.elapsed_time(e1) / 1e3 / steps
-    # FP64 reference of DM rows 0, 700, 1400, 2047 (float32 delay arithmetic)
+    # FP64 reference of four DM rows (0, D/3, 2D/3, D-1; float32 delay arithmetic)
     host = d_in.cpu().numpy().astype(np.float64)
     out = d_out.cpu().numpy().reshape(D, -1)[:, :S]
     live = np.flatnonzero(zapped[:C] == 0)
     err = 0.0
-    for d in (0, 700, 1400, D - 1):
+    for d in sorted({0, D // 3, 2 * D // 3, D - 1}):
         dm = np.float32(obs.getFirstDM()) + np.float32(d) * np.float32(obs.getDMStep())
         delay = (np.float32(dm) * shifts[live].astype(np.float32)).astype(np.uint32)
         ref = np.zeros(S, np.float64)
@@ -797,7 +804,7 @@ def main():
         rates = dd.measure_add_rate(local, 2)
         print(json.dumps(bench_float(torch, local, args.steps,
                                      max(rates["fadd_per_s"], rates["iadd_per_s"]),
-                                     args.float_kernel)))
+                                     args.float_kernel, args.float_dms)))
         return
     if args.subband_only is not None:
         print(json.dumps(subband_only(torch, local, args.subband_only, args.steps, args.warmup)))
