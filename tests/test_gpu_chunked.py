@@ -3,16 +3,16 @@ chunk's input samples are copied in just before it (the first chunk needs
 its tiles plus the largest delay), and its output columns go back to the host
 while later chunks compute.
 
-The result must equal the device plan path bit for bit in single step (3
-synthesized beams, a partial last DM tile and a partial last time tile),
-step one and step two; a small problem keeps one launch and one copy each
-way.
+The result must equal the oracle (include/Dedispersion.hpp:70-176) and the
+device plan path bit for bit in single step (3 synthesized beams, a partial
+last DM tile and a partial last time tile), step one and step two; a small
+problem keeps one launch and one copy each way.
 """
 import numpy as np
 import pytest
 
 import dedispersion_gb300 as dd
-from helpers import engine_run, single_case, step_one_case, step_two_case
+from helpers import engine_run, oracle_run, single_case, step_one_case, step_two_case
 
 pytestmark = pytest.mark.gpu
 
@@ -33,38 +33,38 @@ def _plan_out(case):
     return d_out.cpu().numpy()
 
 
-def test_single_step_chunks_across_beams_and_partial_tiles(gpu):
+def test_single_step_chunks_across_beams_and_partial_tiles(gpu, oracle):
     # 3 synthesized beams x 1000 DMs (a partial last DM tile) x 16300 samples
     # (a partial last time tile): 64 time tiles in 16 chunks, 3072 tiles.
     case = single_case(C=256, D=1000, S=16300, bits=8, padding=128, beams=2, sbeams=3, zap=0.05,
                        seed=17, dist="uniform")
     got = engine_run(case)
-    want = _plan_out(case)
-    np.testing.assert_array_equal(case.valid(got).view(np.uint32),
-                                  case.valid(want).view(np.uint32))
+    for want in (_plan_out(case), oracle_run(oracle, case)):
+        np.testing.assert_array_equal(case.valid(got).view(np.uint32),
+                                      case.valid(want).view(np.uint32))
 
 
-def test_step_one_chunks(gpu):
+def test_step_one_chunks(gpu, oracle):
     case = step_one_case(bits=8, padding=128, seed=5, C=1024, SB=32, D1=64, step1=3.2, D2=16,
                          step2=0.2, S=32000, beams=2, sdisp_multiple=16)
     got = engine_run(case)
-    want = _plan_out(case)
-    np.testing.assert_array_equal(case.valid(got).view(np.uint32),
-                                  case.valid(want).view(np.uint32))
+    for want in (_plan_out(case), oracle_run(oracle, case)):
+        np.testing.assert_array_equal(case.valid(got).view(np.uint32),
+                                      case.valid(want).view(np.uint32))
 
 
-def test_step_two_chunks(gpu):
+def test_step_two_chunks(gpu, oracle):
     case = step_two_case(padding=128, seed=9, float_values=True, C=1024, SB=32, D1=8, D2=256,
                          S=16384, beams=2, sbeams=2)
     got = engine_run(case)
-    want = _plan_out(case)
-    np.testing.assert_array_equal(case.valid(got).view(np.uint32),
-                                  case.valid(want).view(np.uint32))
+    for want in (_plan_out(case), oracle_run(oracle, case)):
+        np.testing.assert_array_equal(case.valid(got).view(np.uint32),
+                                      case.valid(want).view(np.uint32))
 
 
-def test_small_problem_single_launch(gpu):
+def test_small_problem_single_launch(gpu, oracle):
     case = single_case(C=64, D=40, S=512, bits=4, padding=64, sbeams=2, beams=2, seed=3)
     got = engine_run(case)
-    want = _plan_out(case)
-    np.testing.assert_array_equal(case.valid(got).view(np.uint32),
-                                  case.valid(want).view(np.uint32))
+    for want in (_plan_out(case), oracle_run(oracle, case)):
+        np.testing.assert_array_equal(case.valid(got).view(np.uint32),
+                                      case.valid(want).view(np.uint32))

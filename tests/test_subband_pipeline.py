@@ -6,7 +6,11 @@ intermediate (1-8-bit input whose subband sums fit 16 bits: odd and even
 coarse-DM counts, lane widening every few subbands, saturated input) and
 with the float intermediate it falls back to (16-bit input, wide subbands).
 At the full 1536-channel, 32-subband shape the packed pipeline equals the
-engine's own two float steps.
+oracle chain and the engine's own two float steps.  The subband frequencies
+of step two (getShiftsStepTwo) follow AstroData's subband accessors, which
+the reference's sources do not include: the oracle restates them
+(oracle/dd_oracle.c), so step two is pinned to the restatement, not to
+AstroData itself.
 """
 import numpy as np
 import pytest
@@ -144,9 +148,10 @@ def test_host_call_matches_oracle_chain(gpu, oracle):
         np.testing.assert_array_equal(out.reshape(-1, row)[:, :S], want.reshape(-1, row)[:, :S])
 
 
-def test_full_shape_equals_float_steps(gpu):
+def test_full_shape_equals_float_steps(gpu, oracle):
     """1536 channels (5 % zapped), 32 subbands, 64 x 32 DMs, 24576 samples:
-    the packed pipeline equals the engine's float step one + step two."""
+    the packed pipeline equals the oracle's step one + step two and the
+    engine's float step one + step two."""
     torch = pytest.importorskip("torch")
     obs = syn.large_observation(128, subbands=True)
     shifts, shifts2 = dd.getShifts(obs, 128), dd.getShiftsStepTwo(obs, 128)
@@ -175,6 +180,8 @@ def test_full_shape_equals_float_steps(gpu):
     two.run(inter, want)
     two.check()
     assert torch.equal(got, want)
+    ref = _oracle_chain(oracle, obs, shifts, shifts2, zapped, d_in.cpu().numpy(), mapping, 128, 8)
+    assert np.array_equal(got.cpu().numpy().view(np.uint32), ref.view(np.uint32))
     # chunked runs, twice back to back (the second run's step one waits for
     # the first run's step two)
     p.setChunks(6)
