@@ -68,3 +68,38 @@ def test_small_problem_single_launch(gpu, oracle):
     for want in (_plan_out(case), oracle_run(oracle, case)):
         np.testing.assert_array_equal(case.valid(got).view(np.uint32),
                                       case.valid(want).view(np.uint32))
+
+
+def _pinned_like(out):
+    torch = pytest.importorskip("torch")
+    t = torch.full((out.size,), -3.0, dtype=torch.float32).pin_memory()
+    return t, t.numpy()
+
+
+@pytest.mark.parametrize("kind", ["single_chunked", "single_small", "step_one_chunked"])
+def test_pinned_output_written_by_the_kernels(gpu, oracle, kind):
+    """With a pinned host output on a device that reaches host memory through
+    the host's page tables, the kernels write the output straight into it
+    (no device buffer, no copy back); the result is the oracle's bit for bit
+    and the row padding is left as it was."""
+    if kind == "single_chunked":
+        case = single_case(C=256, D=1000, S=16300, bits=8, padding=128, beams=2, sbeams=3,
+                           zap=0.05, seed=19)
+    elif kind == "single_small":
+        case = single_case(C=64, D=40, S=500, bits=4, padding=64, sbeams=2, beams=2, seed=23)
+    else:
+        case = step_one_case(bits=8, padding=128, seed=29, C=1024, SB=32, D1=64, step1=3.2,
+                             D2=16, step2=0.2, S=32000, beams=2, sdisp_multiple=16)
+    keep, out = _pinned_like(case.output())
+    if case.mode == dd.DD_SINGLE_STEP:
+        dd.dedispersion(case.obs, case.zapped, case.mapping, case.inp, out, case.shifts,
+                        case.padding, case.bits)
+    else:
+        dd.subbandDedispersionStepOne(case.obs, case.zapped, case.inp, out, case.shifts,
+                                      case.padding, case.bits)
+    want = oracle_run(oracle, case)
+    np.testing.assert_array_equal(case.valid(out).view(np.uint32),
+                                  case.valid(want).view(np.uint32))
+    pad = out.reshape(case.out_rows, case.out_row)[:, case.nr_samples:]
+    assert (pad == -3.0).all()
+    del keep
