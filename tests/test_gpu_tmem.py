@@ -95,3 +95,43 @@ def test_wide_spread_falls_back_to_scalar(gpu, oracle):
     with pytest.raises(dd.DedispersionError) as e:
         _run(case, kernel=TMEM)
     assert "16 DMs spread a row's delay" in str(e.value)
+
+
+def test_full_size_float_rows(gpu, oracle):
+    """The 1536 ch x 2048 DM x 24576-sample workload with float32 input
+    (N(128, 20), 5 % zapped): every DM row equals the scalar tile's bit for
+    bit, and 64 DM rows spread over the range equal the oracle's."""
+    torch = pytest.importorskip("torch")
+    from dedispersion_gb300 import synthetic as syn
+    obs = syn.large_observation(128)
+    shifts = dd.getShifts(obs, 128)
+    zapped = syn.zapped_mask(1536, 0.05, 7, 128)
+    mapping = syn.identity_mapping(obs, 128)
+    lay = dd.layout(obs, dd.DD_SINGLE_STEP, 32, 128)
+    rng = np.random.default_rng(41)
+    row = lay.input_row_bytes // 4
+    inp = np.zeros((1536, row), np.float32)
+    n = obs.getNrSamplesPerDispersedBatch()
+    inp[:, :n] = rng.normal(128.0, 20.0, size=(1536, n)).astype(np.float32)
+    d_in = torch.from_numpy(inp).cuda()
+    outs = {}
+    for name in (TMEM, SCALAR):
+        p = dd.Plan(obs, dd.DD_SINGLE_STEP, 32, 128, kernel=_kernel(name))
+        p.setShifts(shifts)
+        p.setZappedChannels(zapped)
+        p.setBeamMapping(mapping)
+        d_out = torch.full((lay.output_bytes // 4,), -1.0, dtype=torch.float32, device="cuda")
+        p.run(d_in, d_out)
+        p.check()
+        p.close()
+        outs[name] = d_out.cpu().numpy()
+    D, S = obs.getNrDMs(), obs.getNrSamplesPerBatch()
+    a = outs[TMEM].reshape(D, -1)[:, :S]
+    b = outs[SCALAR].reshape(D, -1)[:, :S]
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    want = np.zeros(lay.output_bytes // 4, np.float32)
+    for d in np.linspace(0, D - 1, 64).astype(int):
+        oracle.dedispersion(obs.c, zapped, mapping, inp, want, shifts, 128, 32,
+                            dm_begin=int(d), dm_end=int(d) + 1)
+        w = want.reshape(D, -1)[d, :S]
+        assert np.array_equal(a[d].view(np.uint32), w.view(np.uint32)), f"DM row {d}"
