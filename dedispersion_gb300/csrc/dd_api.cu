@@ -287,6 +287,10 @@ struct dd_plan {
   dd::EntryDesc *d_entries = nullptr;
   size_t cap_groups = 0, cap_entries = 0;
   uint32_t *d_status = nullptr;
+  // TMEM-window tile offsets (ProblemDesc::tmem_tab).
+  std::vector<uint32_t> tmem_tab;
+  uint32_t *d_tmem_tab = nullptr;
+  size_t cap_tmem_tab = 0;
   // Precomputed delays (ProblemDesc::delay_base / delay_rel).
   std::vector<float> delay_shift;  // delay per unit DM of each delay row
   std::vector<uint16_t> delay_rel;
@@ -486,6 +490,7 @@ dd_status rebuild(dd_plan *p) {
     if (!dd::tmem_fits(uniq.data(), uniq.size(), d.first_dm, d.dm_step, d.nr_dms))
       return fail(DD_ERR_UNSUPPORTED, "tile %s: 16 DMs spread a row's delay by more than %u "
                   "samples", k.name, dd::kTmMaxOff - 3u);
+    dd::tmem_tables(p->delay_shift, d.first_dm, d.dm_step, d.nr_dms, &p->tmem_tab);
   }
   if (shared) {
     if (p->mode != DD_SINGLE_STEP || p->bits > 8)
@@ -560,9 +565,22 @@ dd_status rebuild(dd_plan *p) {
   if (!p->entries.empty())
     DD_CUDA(cudaMemcpy(p->d_entries, p->entries.data(), p->entries.size() * sizeof(dd::EntryDesc),
                        cudaMemcpyHostToDevice), "upload entry table");
+  if (tmem) {
+    if (p->tmem_tab.size() > p->cap_tmem_tab || !p->d_tmem_tab) {
+      if (p->d_tmem_tab) cudaFree(p->d_tmem_tab);
+      p->d_tmem_tab = nullptr;
+      DD_CUDA(cudaMalloc(&p->d_tmem_tab, std::max<size_t>(1, p->tmem_tab.size()) * sizeof(uint32_t)),
+              "allocate TMEM tile offsets");
+      p->cap_tmem_tab = std::max<size_t>(1, p->tmem_tab.size());
+    }
+    if (!p->tmem_tab.empty())
+      DD_CUDA(cudaMemcpy(p->d_tmem_tab, p->tmem_tab.data(), p->tmem_tab.size() * sizeof(uint32_t),
+                         cudaMemcpyHostToDevice), "upload TMEM tile offsets");
+  }
   if (p->use_delay_tables) {
     if (p->delay_rel.size() > p->cap_delay_rel) {
       if (p->d_delay_rel) cudaFree(p->d_delay_rel);
+    if (p->d_tmem_tab) cudaFree(p->d_tmem_tab);
       p->d_delay_rel = nullptr;
       DD_CUDA(cudaMalloc(&p->d_delay_rel, p->delay_rel.size() * sizeof(uint16_t)),
               "allocate delay table");
@@ -847,6 +865,10 @@ dd_status plan_problem(const dd_plan *p, const void *d_input, float *d_output,
   if (p->use_delay_tables) {
     P.delay_rows = (uint32_t)p->delay_shift.size();
     P.delay_rel = p->d_delay_rel;
+  }
+  if (p->kinfo->family == kFamilyTmem32) {
+    P.delay_rows = (uint32_t)p->delay_shift.size();
+    P.tmem_tab = reinterpret_cast<const uint4 *>(p->d_tmem_tab);
   }
   if (p->packed) {
     const uint32_t D1 = p->obs.nr_dms_subbanding;
@@ -1325,6 +1347,7 @@ dd_status dd_plan_destroy(dd_plan *p) {
     if (p->d_entries) cudaFree(p->d_entries);
     if (p->d_status) cudaFree(p->d_status);
     if (p->d_delay_rel) cudaFree(p->d_delay_rel);
+    if (p->d_tmem_tab) cudaFree(p->d_tmem_tab);
     if (p->d_stage_rows) cudaFree(p->d_stage_rows);
     if (p->d_tile_stage) cudaFree(p->d_tile_stage);
     if (p->d_pool) cudaFree(p->d_pool);

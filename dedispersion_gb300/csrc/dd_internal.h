@@ -135,6 +135,9 @@ struct ProblemDesc {
   // (dd_plan_set_wait_limit).  The drain after a timeout keeps its own
   // limit, so every copy in flight lands before a CTA exits.
   uint32_t wait_ns;
+  // kFamilyTmem32: the offsets of every (DM tile, delay row), 20 words each
+  // (dd_tmem.cuh, tmem_tables); rows are entries' delay_row.
+  const uint4 *tmem_tab;
 };
 
 // One entry of the kernel registry: a compiled tile configuration.

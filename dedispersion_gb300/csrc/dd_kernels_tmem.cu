@@ -61,7 +61,8 @@ __global__ void __launch_bounds__(kTmThreads, 1) tmem32_kernel(const ProblemDesc
   extern __shared__ __align__(128) uint8_t smem[];
   __shared__ uint64_t bars[kTmSlots];
   __shared__ uint32_t tbase_s;
-  __shared__ __align__(16) uint32_t tab[4][kTmRows][kTmTabWords];
+  // Offsets of each slot's rows (tmem_tables), fetched with the rows.
+  __shared__ __align__(16) uint32_t tab[kTmSlots][kTmRows][kTmTabWords];
   const int tid = threadIdx.x, w = tid >> 5, tx = tid & 31, q = w & 3, k = w >> 2;
   uint32_t g, dtile, ttile;
   decode_tile(P, blockIdx.x, g, dtile, ttile);
@@ -72,6 +73,7 @@ __global__ void __launch_bounds__(kTmThreads, 1) tmem32_kernel(const ProblemDesc
   const uint32_t base = smem_addr(smem);
   float *shift_s = reinterpret_cast<float *>(smem + kTmSlots * kTmSlotBytes);
   uint32_t *chunk_s = reinterpret_cast<uint32_t *>(shift_s + P.win_samples);
+  uint32_t *drow_s = chunk_s + P.win_samples;
 
   if (w == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
@@ -87,6 +89,7 @@ __global__ void __launch_bounds__(kTmThreads, 1) tmem32_kernel(const ProblemDesc
     const EntryDesc E = P.entries[G.entry_begin + r];
     shift_s[r] = E.shift;
     chunk_s[r] = static_cast<uint32_t>(E.row_offset >> 4);  // 16-byte rows when P.tma
+    drow_s[r] = E.delay_row;
   }
   tm_fence_before();
   __syncthreads();
@@ -94,53 +97,48 @@ __global__ void __launch_bounds__(kTmThreads, 1) tmem32_kernel(const ProblemDesc
   const uint32_t tbase = tbase_s;
   const uint32_t tmem = tbase + ((uint32_t)(32 * q) << 16);
 
-  // Offset table of step u (threads 0..255: one (row, quarter, DM) each):
-  // word 0 the window start in bytes from the row start, 1 the row, 2 + q
-  // quarter q's window start in chunks, 6 + q its TMEM columns to stage,
-  // 10 + 4q + k the offsets of warp k's 4 DMs (bytes).
-  auto table = [&](uint32_t u) {
-    if (tid >= kTmRows * 64) return;
-    const uint32_t rr = tid >> 6, qq = (tid >> 4) & 3u, j = tid & 15u;
-    const uint32_t r = u * kTmRows + rr;
-    if (r >= nrows) return;
-    uint32_t *e = tab[u & 3][rr];
-    const float sh = shift_s[r];
-    const uint32_t last = P.nr_dms - 1;
-    const uint32_t w0 = (t0 + dev_delay(P.first_dm, P.dm_step, d0, sh)) & ~3u;
-    const uint32_t dq = min(d0 + 16u * qq, last);
-    const uint32_t wq = (t0 + dev_delay(P.first_dm, P.dm_step, dq, sh)) & ~3u;
-    const uint32_t d = min(d0 + 16u * qq + j, last);
-    const uint32_t o = min(t0 + dev_delay(P.first_dm, P.dm_step, d, sh) - wq, kTmMaxOff);
-    const uint32_t offq = min((wq - w0) >> 2, kTmMaxQuarterOff);
-    reinterpret_cast<uint8_t *>(e + 10 + 4 * qq)[j] = (uint8_t)o;
-    if (j == 0) e[2 + qq] = offq;
-    if (j == 15) e[6 + qq] = (o + kTmT + 15u) & ~15u;
-    if (qq == 0 && j == 0) {
-      e[0] = w0 * 4u;
-      e[1] = r;
-    }
-  };
   // Copies of step u into slot u % 3: thread tid copies chunks
-  // (tid & 127) + 128 i of row tid >> 7, then arrives once on the slot.
+  // (tid & 127) + 128 i of row tid >> 7 (the window from
+  // W_0 = t0 + B), threads 0..19 also the rows' offset entries, then every
+  // thread arrives once on the slot.
   const uint32_t crow = tid >> 7, cc = tid & 127;
   auto copy = [&](uint32_t u) {
     const uint32_t slot = u % kTmSlots;
     const uint32_t r = u * kTmRows + crow;
+    if (tid < kTmRows * kTmTabChunks) {
+      const uint32_t rr = tid / kTmTabChunks, c = tid % kTmTabChunks;
+      const uint32_t rt = u * kTmRows + rr;
+      if (rt < nrows && P.tma)
+        cp_async16_tm(smem_addr(&tab[slot][rr][4 * c]),
+                      P.tmem_tab + ((size_t)dtile * P.delay_rows + drow_s[rt]) * kTmTabChunks + c,
+                      16u);
+      else if (rt < nrows)
+        *reinterpret_cast<uint4 *>(&tab[slot][rr][4 * c]) =
+            P.tmem_tab[((size_t)dtile * P.delay_rows + drow_s[rt]) * kTmTabChunks + c];
+    }
     if (r < nrows) {
-      const uint32_t *e = tab[u & 3][crow];
-      const uint32_t rel = e[0];
+      const uint32_t rel = (t0 + (dev_delay(P.first_dm, P.dm_step, d0, shift_s[r]) & ~3u)) * 4u;
       const uint32_t dst = base + slot * kTmSlotBytes + crow * kTmRowBytes;
       if (P.tma) {
-        const uint8_t *src = P.in + (uint64_t)chunk_s[r] * 16u;
+        const uint8_t *src = P.in + (uint64_t)chunk_s[r] * 16u + rel;
+        if ((uint64_t)rel + 16u * kTmChunks <= P.row_bytes) {
+          // The whole window lies inside the row.
 #pragma unroll
-        for (int i = 0; i < 2; ++i) {
-          const uint32_t c = cc + 128u * i;
-          if (c < kTmChunks) {
-            const uint64_t off = (uint64_t)rel + 16u * c;
-            const uint32_t n = P.row_bytes > off
-                                   ? (P.row_bytes - off < 16u ? (uint32_t)(P.row_bytes - off) : 16u)
-                                   : 0u;
-            cp_async16_tm(dst + tm_chunk(c), n ? src + off : src, n);
+          for (int i = 0; i < 2; ++i) {
+            const uint32_t c = cc + 128u * i;
+            if (c < kTmChunks) cp_async16_tm(dst + tm_chunk(c), src + 16u * c, 16u);
+          }
+        } else {
+#pragma unroll
+          for (int i = 0; i < 2; ++i) {
+            const uint32_t c = cc + 128u * i;
+            if (c < kTmChunks) {
+              const uint64_t off = (uint64_t)rel + 16u * c;
+              const uint32_t n = P.row_bytes > off
+                                     ? (P.row_bytes - off < 16u ? (uint32_t)(P.row_bytes - off) : 16u)
+                                     : 0u;
+              cp_async16_tm(dst + tm_chunk(c), n ? src + 16u * c : P.in, n);
+            }
           }
         }
       } else {
@@ -170,8 +168,6 @@ __global__ void __launch_bounds__(kTmThreads, 1) tmem32_kernel(const ProblemDesc
       mbar_arrive(bars + slot);
   };
 
-  for (uint32_t u = 0; u < 3 && u < nst; ++u) table(u);
-  __syncthreads();
   if (nst > 0) copy(0);
   if (nst > 1) copy(1);
 
@@ -191,9 +187,9 @@ __global__ void __launch_bounds__(kTmThreads, 1) tmem32_kernel(const ProblemDesc
       // Warp k copies columns 16k .. 16k + 15 of its quarter's windows.
       const uint32_t sb = base + slot * kTmSlotBytes;
       for (uint32_t r = 0; r < nr; ++r) {
-        const uint32_t *e = tab[s & 3][r];
-        if (16u * k >= e[6 + q]) continue;  // warp-uniform: no DM reaches these columns
-        const uint32_t g0 = e[2 + q] + 4u * tx + 4u * k;
+        const uint32_t *e = tab[slot][r];
+        if (16u * k >= ((e[2] >> (8 * q)) & 0xFFu)) continue;  // warp-uniform: no DM reaches these columns
+        const uint32_t g0 = ((e[1] >> (8 * q)) & 0xFFu) + 4u * tx + 4u * k;
         uint32_t v[16];
 #pragma unroll
         for (int m = 0; m < 4; ++m) {
@@ -213,10 +209,9 @@ __global__ void __launch_bounds__(kTmThreads, 1) tmem32_kernel(const ProblemDesc
       break;
     }
     tm_fence_after();
-    if (s + 3 < nst) table(s + 3);
     if (s + 2 < nst) copy(s + 2);
     for (uint32_t r = 0; r < nr; ++r) {
-      const uint32_t ow = tab[s & 3][r][10 + 4 * q + k];
+      const uint32_t ow = tab[slot][r][4 + 4 * q + k];
       const uint32_t col = tmem + buf * 256u + r * kTmCols;
 #pragma unroll
       for (int j = 0; j < kTmDPW; j += 2) {

@@ -35,6 +35,7 @@
 #include <algorithm>
 #include <cstddef>
 #include <cstdint>
+#include <vector>
 
 #include "dd_internal.h"
 
@@ -53,13 +54,15 @@ constexpr uint32_t kTmMaxQuarterOff = kTmChunks - 4 * 31 - 16;  // 52 chunks
 constexpr uint32_t kTmRowBytes = (kTmChunks + kTmChunks / 8) * 16;  // 3456
 constexpr uint32_t kTmSlots = 3;
 constexpr uint32_t kTmSlotBytes = kTmRows * kTmRowBytes;
-constexpr uint32_t kTmTabWords = 32;  // per row: rel, row, off[4], cols[4], 16 DM offset words
+
+constexpr uint32_t kTmTabWords = 20;  // per (DM tile, delay row): see tmem_tables
+constexpr uint32_t kTmTabChunks = kTmTabWords / 4;
 
 // Dynamic shared memory of a launch whose groups have at most `rows` rows:
-// the staging slots, then each row's delay per unit DM and 16-byte chunk
-// index.
+// the staging slots, then each row's delay per unit DM, 16-byte chunk index
+// and delay-table row.
 __host__ __device__ inline size_t tmem_smem_bytes(uint32_t rows) {
-  return (size_t)kTmSlots * kTmSlotBytes + 8u * (size_t)rows;
+  return (size_t)kTmSlots * kTmSlotBytes + 12u * (size_t)rows;
 }
 
 // Whether every row's windows fit the tile: within each quarter's 16 DMs the
@@ -83,6 +86,41 @@ inline bool tmem_fits(const float *shifts, size_t n, float first_dm, float dm_st
       }
     }
   return true;
+}
+
+// The tile's offsets of every (DM tile, delay row), 20 words each, so that
+// the kernel fetches them with the row instead of evaluating delays: word 0
+// the delay of the tile's first DM rounded down to 4 samples (B), word 1
+// byte q each quarter's window start (W_q - B) / 4 in chunks, word 2 byte q
+// the TMEM columns quarter q stages (a multiple of 16), word 4 + 4q + k
+// bytes j the offset o of DM 16q + 4k + j.  Time tiles start at multiples of
+// 512 samples, so none of these depends on the time tile.  Host delays round
+// as the device's (host_delay).
+inline void tmem_tables(const std::vector<float> &row_shift, float first_dm, float dm_step,
+                        uint32_t nr_dms, std::vector<uint32_t> *out) {
+  const uint32_t tiles = nr_dms ? (nr_dms + kTmTileD - 1) / kTmTileD : 0;
+  const size_t rows = row_shift.size();
+  out->assign((size_t)tiles * rows * kTmTabWords, 0u);
+  for (uint32_t t = 0; t < tiles; t++)
+    for (size_t r = 0; r < rows; r++) {
+      const float sh = row_shift[r];
+      uint32_t *e = out->data() + ((size_t)t * rows + r) * kTmTabWords;
+      const uint32_t d0 = t * kTmTileD, last = nr_dms - 1;
+      const uint32_t b = host_delay(first_dm, dm_step, d0, sh) & ~3u;
+      e[0] = b;
+      for (uint32_t q = 0; q < 4; q++) {
+        const uint32_t wq = host_delay(first_dm, dm_step, std::min(d0 + 16u * q, last), sh) & ~3u;
+        uint32_t omax = 0;
+        for (uint32_t j = 0; j < 16; j++) {
+          const uint32_t d = std::min(d0 + 16u * q + j, last);
+          const uint32_t o = std::min(host_delay(first_dm, dm_step, d, sh) - wq, kTmMaxOff);
+          omax = std::max(omax, o);
+          e[4 + 4 * q + j / 4] |= o << (8 * (j % 4));
+        }
+        e[1] |= std::min((wq - b) / 4u, kTmMaxQuarterOff) << (8 * q);
+        e[2] |= ((omax + kTmT + 15u) & ~15u) << (8 * q);
+      }
+    }
 }
 
 }  // namespace dd
