@@ -24,6 +24,7 @@ from __future__ import annotations
 import argparse
 import dataclasses
 import json
+import functools
 import math
 import sys
 import time
@@ -224,12 +225,49 @@ def measured_observation(s: Shape, padding: int, max_dms: int = 1024,
 FEATURE_NAMES = ("log2 channels", "log2 rows", "log2 dms", "log2 samples", "log2 subbands+1",
                  "log2 spread", "log2 sharing", "log2 items d0", "log2 items d1",
                  "log2 warps d1", "log2 unroll", "log2 tile dms", "log2 tile samples",
-                 "subband", "log2 waves", "wave efficiency", "short groups") + \
+                 "subband", "log2 waves", "wave efficiency", "short groups",
+                 "log2 shared adds ratio") + \
     tuple(f"bits {b}" for b in BITS) + \
     tuple(f"variant {v}" for v in VARIANTS) + tuple(f"family {f}" for f in FAMILIES)
 
 
 GPU_SMS = 152  # SMs of a GB300
+
+
+@functools.lru_cache(maxsize=4096)
+def shared_adds_ratio(channels: int, dms: int, dm_step: float, tile_d: int,
+                      samples_sub: int = 12, samples_tile: int = 4) -> float:
+    """Estimated integer adds of the shared-partial-sum tile per direct-sum
+    add, for a single-step shape of the study band (1220-1520 MHz at 81.92
+    us): rows in subgroups of 8, per DM tile each distinct relative-delay
+    vector of a subgroup summed once (its first vector over its 8 rows, each
+    next one from the previous with 2 adds per moved row, in DM order) and
+    one series add per DM and subgroup.  Evaluated on `samples_sub` subgroups
+    x `samples_tile` DM tiles spread over the shape (about a millisecond), in
+    the reference's float order for the delays."""
+    bw = 300.0 / channels
+    f = 1220.0 + np.arange(channels, dtype=np.float64) * bw
+    shift = (4148.808 * (1.0 / f ** 2 - 1.0 / f[-1] ** 2) / 81.92e-6).astype(np.float32)
+    dms = max(1, min(dms, 1024))
+    nsub = max(1, channels // 8)
+    tiles = max(1, -(-dms // tile_d))
+    subs = np.unique(np.linspace(0, nsub - 1, min(nsub, samples_sub)).astype(int))
+    tl = np.unique(np.linspace(0, tiles - 1, min(tiles, samples_tile)).astype(int))
+    rows = shift[(8 * subs[:, None] + np.arange(8)[None, :]).clip(max=channels - 1)]  # [g, 8]
+    weights = (np.int64(1) << (np.arange(8, dtype=np.int64) * 7))
+    cost = 0.0
+    for t in tl:
+        dm = np.minimum(np.arange(t * tile_d, (t + 1) * tile_d), dms - 1).astype(np.float32)
+        val = (dm * np.float32(dm_step)).astype(np.float32)
+        d = (rows[:, :, None] * val[None, None, :]).astype(np.float32).astype(np.int64)
+        rel = d - d.min(axis=1, keepdims=True)                                # [g, 8, D]
+        keys = (np.minimum(rel, 127) * weights[None, :, None]).sum(axis=1)  # [g, D]
+        for gi in range(len(subs)):
+            _, first = np.unique(keys[gi], return_index=True)
+            v = rel[gi][:, np.sort(first)]                                   # distinct, DM order
+            moves = int((v[:, 1:] != v[:, :-1]).sum())
+            cost += (8 + 2 * moves) / (8 * tile_d)
+    return float(1.0 / 8 + cost / (len(tl) * len(subs)))
 
 
 def resident_ctas(name: str, conf: DedispersionConf) -> int:
@@ -265,7 +303,9 @@ def features(s: Shape, conf: DedispersionConf, name: str) -> np.ndarray:
          math.log2(conf.nrItemsD0), math.log2(conf.nrItemsD1), math.log2(conf.nrThreadsD1),
          math.log2(conf.unroll), math.log2(tile_d), math.log2(tile_t),
          float(s.subbands > 0), math.log2(1 + waves), waves / math.ceil(waves),
-         float(name.startswith("swar8s"))]
+         float(name.startswith("swar8s")),
+         math.log2(shared_adds_ratio(s.channels, s.dms, s.dm_step, tile_d))
+         if name.startswith("shared8") else 0.0]
     f += [float(s.bits == b) for b in BITS]
     f += [float(name.endswith("_vkUnpack" + v)) for v in VARIANTS]
     f += [float(name.startswith(fam)) for fam in FAMILIES]
