@@ -22,7 +22,9 @@
 //
 // Per step of 4 rows: 16-byte asynchronous copies stage each row's window
 // (768 floats from W_0, one pad chunk per 8 so that the lanes' 16-byte loads
-// at a 64-byte stride spread over the banks) into one of 3 slots; every warp
+// at a 64-byte stride spread over the banks) and its offset entry (built on
+// the host by tmem_tables: W_q - W_0, the columns to stage and every DM's o)
+// into one of 3 slots; every warp
 // copies 16 of its quarter's 64 columns into TMEM (tcgen05.st; only the
 // columns the row's DMs reach); after a block barrier the warps add from
 // TMEM while the next rows' copies are in flight.  Two TMEM buffers of 4

@@ -185,7 +185,10 @@ dd_status dd_write_tuned_conf(const char *path, const char *device,
 /* ---- synchronous host-buffer calls -------------------------------------- */
 /* Drop-in replacements of the reference's CPU templates.  Host pointers in
  * the reference layout; the call copies to the device, runs, copies the
- * result back and returns when `output` holds it. */
+ * result back and returns when `output` holds it.  An `output` in pinned
+ * host memory on a device that reaches host memory through the host's page
+ * tables (a Grace host) is written by the kernels directly, without a copy
+ * back; the result is the same. */
 
 /* Dedispersion::dedispersion<I,L,O> (include/Dedispersion.hpp:59, 70-109). */
 dd_status dd_dedispersion(const dd_observation *obs, const uint32_t *zapped,
@@ -303,7 +306,10 @@ typedef struct dd_plan dd_plan;
  * other direct tiles of the input width, largest first.  For single-step
  * 1-8-bit input the default is the shared-partial-sum tile while its
  * executed adds stay below 0.34 of the direct sum, else the direct default
- * (measured crossover).  `device` is a CUDA device index. */
+ * (measured crossover).  For single-step float input it is the TMEM-window
+ * tile (items_d2 = 3; same float order as the scalar tile, bit-identical)
+ * where 16 DMs move a row's delay by at most 45 samples, else the scalar
+ * tile.  `device` is a CUDA device index. */
 dd_status dd_plan_create(dd_plan **plan, const dd_observation *obs,
                          dd_mode mode, uint32_t input_bits, uint32_t padding,
                          const dd_conf *conf, int device);
@@ -348,7 +354,8 @@ dd_status dd_plan_adds(const dd_plan *plan, uint64_t *adds);
  * previous launch to complete before it writes anything.  Only for runs whose
  * input is not written by the kernel launched just before them on the stream
  * (consecutive independent batches).  Applies to the shared-partial-sum and
- * 1/2/4/8-bit direct kernels; the 16-bit and float kernels launch as usual.
+ * 1/2/4/8-bit direct kernels; the 16-bit and float kernels (scalar and
+ * TMEM-window) launch as usual.
  * Off by default. */
 /* Limit, in nanoseconds, of each bounded device-side wait for a staged
  * copy in this plan's runs (0, the default: 2 s).  When a wait runs out the
