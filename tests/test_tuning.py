@@ -141,3 +141,23 @@ def test_observation_shape_maps_problems_to_study_features(engine):
 def _first(shape):
     k = tuning.family_kernels(shape.mode(), shape.bits)[0]
     return k.conf, k.name
+
+
+def test_shared_adds_ratio_estimate(engine):
+    """The shared tile's estimated adds per direct-sum add: at least the
+    series adds (1/8), below the direct sum for the study band, rising with
+    the DM step (fewer DMs share a delay vector), and the feature is set for
+    the shared configurations only."""
+    r = [tuning.shared_adds_ratio(1536, 2048, s, 64) for s in (0.05, 0.2, 0.45)]
+    assert all(0.125 < x < 1.0 for x in r)
+    assert r[0] < r[1] < r[2]
+    # 1536 channels, 2048 DMs at 0.2: the plans' own count is 0.21-0.23
+    assert 0.18 < r[1] < 0.30
+    s = tuning.Shape(channels=1536, dms=2048, samples=24576, bits=8, subbands=0, dm_step=0.2)
+    i = tuning.FEATURE_NAMES.index("log2 shared adds ratio")
+    for k in tuning.family_kernels(s.mode(), s.bits):
+        f = tuning.features(s, k.conf, k.name)
+        if k.name.startswith("shared8"):
+            assert f[i] < 0
+        else:
+            assert f[i] == 0
