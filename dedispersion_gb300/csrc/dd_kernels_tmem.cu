@@ -7,6 +7,14 @@ namespace dd {
 
 // 16 columns of this warp's 32 lanes from registers (tcgen05.st, shape
 // 32x32b: thread i writes lane i, register j to column taddr + j).
+__device__ __forceinline__ void tm_st8(uint32_t taddr, const uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};"
+      :: "r"(taddr), "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]),
+         "r"(v[6]), "r"(v[7])
+      : "memory");
+}
+
 __device__ __forceinline__ void tm_st16(uint32_t taddr, const uint32_t (&v)[16]) {
   asm volatile(
       "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16};"
@@ -184,22 +192,29 @@ __global__ void __launch_bounds__(kTmThreads, 1) tmem32_kernel(const ProblemDesc
     const uint32_t nr = min(nrows - s * kTmRows, (uint32_t)kTmRows);
     const bool landed = mbar_wait(bars + slot, (s / kTmSlots) & 1u, kWaitNs, P.wait_ns);
     if (landed) {
-      // Warp k copies columns 16k .. 16k + 15 of its quarter's windows.
+      // Warp k copies columns 16k .. 16k + 15 of its quarter's windows, or
+      // the first 8 of them where the row's DMs reach no further.
       const uint32_t sb = base + slot * kTmSlotBytes;
       for (uint32_t r = 0; r < nr; ++r) {
         const uint32_t *e = tab[slot][r];
-        if (16u * k >= ((e[2] >> (8 * q)) & 0xFFu)) continue;  // warp-uniform: no DM reaches these columns
+        const uint32_t cols = (e[2] >> (8 * q)) & 0xFFu;
+        if (16u * k >= cols) continue;  // warp-uniform: no DM reaches these columns
+        const bool half = 16u * k + 8u >= cols;
         const uint32_t g0 = ((e[1] >> (8 * q)) & 0xFFu) + 4u * tx + 4u * k;
         uint32_t v[16];
 #pragma unroll
         for (int m = 0; m < 4; ++m) {
+          if (m >= 2 && half) break;
           const uint4 x = lds128_tm(sb + r * kTmRowBytes + tm_chunk(g0 + m));
           v[4 * m] = x.x;
           v[4 * m + 1] = x.y;
           v[4 * m + 2] = x.z;
           v[4 * m + 3] = x.w;
         }
-        tm_st16(tmem + buf * 256u + r * kTmCols + 16u * k, v);
+        if (half)
+          tm_st8(tmem + buf * 256u + r * kTmCols + 16u * k, v);
+        else
+          tm_st16(tmem + buf * 256u + r * kTmCols + 16u * k, v);
       }
       asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
     }

@@ -94,7 +94,7 @@ inline bool tmem_fits(const float *shifts, size_t n, float first_dm, float dm_st
 // the kernel fetches them with the row instead of evaluating delays: word 0
 // the delay of the tile's first DM rounded down to 4 samples (B), word 1
 // byte q each quarter's window start (W_q - B) / 4 in chunks, word 2 byte q
-// the TMEM columns quarter q stages (a multiple of 16), word 4 + 4q + k
+// the TMEM columns quarter q stages (a multiple of 8), word 4 + 4q + k
 // bytes j the offset o of DM 16q + 4k + j.  Time tiles start at multiples of
 // 512 samples, so none of these depends on the time tile.  Host delays round
 // as the device's (host_delay).
@@ -120,7 +120,7 @@ inline void tmem_tables(const std::vector<float> &row_shift, float first_dm, flo
           e[4 + 4 * q + j / 4] |= o << (8 * (j % 4));
         }
         e[1] |= std::min((wq - b) / 4u, kTmMaxQuarterOff) << (8 * q);
-        e[2] |= ((omax + kTmT + 15u) & ~15u) << (8 * q);
+        e[2] |= ((omax + kTmT + 7u) & ~7u) << (8 * q);
       }
     }
 }
