@@ -1383,10 +1383,14 @@ constexpr uint64_t kChunkMinTiles = 2048;
 // host memory took 2.78 ms against 2.75 ms into device memory.
 void *host_output_device_address(void *host, size_t bytes, int dev) {
   if (!host || bytes == 0) return nullptr;
-  int pageable = 0;
-  if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
-    (void)cudaGetLastError();
-    return nullptr;
+  // The device attribute, read once per thread (run_sync's cache is per
+  // thread too; it always runs on device 0).
+  thread_local int pageable = -1;
+  if (pageable < 0) {
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
+      (void)cudaGetLastError();
+      pageable = 0;
+    }
   }
   if (!pageable) return nullptr;
   cudaPointerAttributes a{}, b{};
@@ -1496,7 +1500,10 @@ dd_status run_sync(const dd_observation *o, dd_mode mode, const uint32_t *zapped
     DD_CUDA(cudaMalloc(&c.d_in, in_bytes), "allocate device input");
     c.cap_in = in_bytes;
   }
-  if (out_bytes > c.cap_out) {
+  // Pinned host output on a Grace host: the kernels write it directly, and
+  // no device output buffer is needed.
+  float *direct = static_cast<float *>(host_output_device_address(output, out_bytes, 0));
+  if (!direct && out_bytes > c.cap_out) {
     if (c.d_out) cudaFree(c.d_out);
     c.d_out = nullptr; c.cap_out = 0;
     DD_CUDA(cudaMalloc(&c.d_out, out_bytes), "allocate device output");
@@ -1505,8 +1512,6 @@ dd_status run_sync(const dd_observation *o, dd_mode mode, const uint32_t *zapped
   const dd_plan *p = c.plan;
   const uint64_t tt_total = p->tiles_t;
   const uint64_t tiles = (uint64_t)p->nr_groups * p->tiles_d * tt_total;
-  // Pinned host output on a Grace host: the kernels write it directly.
-  float *direct = static_cast<float *>(host_output_device_address(output, out_bytes, 0));
   float *kout = direct ? direct : c.d_out;
   if (tiles < kChunkMinTiles || tt_total < 2 || !d.nr_samples || !d.output_rows) {
     // Small problems: one copy in, one launch, one copy out.
