@@ -1,5 +1,6 @@
 """Real-time serving: admission by device-memory budget, and every served
-batch equal to the plain path on its window [tail | batch]."""
+batch equal to the oracle (include/Dedispersion.hpp:70-176) on its window
+[tail | batch]."""
 import dataclasses
 
 import numpy as np
@@ -49,8 +50,9 @@ def batch_data(cfg, k):
     return syn.pack_subbyte(vals.astype(np.uint8), cfg.bits, cfg.samples * cfg.bits // 8)
 
 
-def plain_reference(stream, window):
-    """The plain path (synchronous C ABI calls) on one [tail | batch] window."""
+def plain_reference(stream, window, oracle):
+    """The oracle (the CPU restatement of the reference's loops) on one
+    [tail | batch] window: single step, or step one then step two."""
     cfg = stream.cfg
     obs = stream.obs.copy()
     S = cfg.samples
@@ -61,8 +63,8 @@ def plain_reference(stream, window):
         inp[:, :window.shape[1]] = window
         out = np.zeros(lay.output_bytes // 4, np.float32)
         mapping = np.zeros(lay.mapping_row_elems, np.uint32)
-        dd.dedispersion(obs, stream.zapped, mapping, inp.reshape(-1), out, stream.shifts,
-                        cfg.padding, cfg.bits)
+        oracle.dedispersion(obs.c, stream.zapped, mapping, inp.reshape(-1), out, stream.shifts,
+                            cfg.padding, cfg.bits)
         return out.reshape(-1, lay.output_row_elems)[:, :S]
     s1 = S + serving_tail_step_two(stream)
     obs.setNrSamplesPerBatch(s1, True)
@@ -71,12 +73,12 @@ def plain_reference(stream, window):
     inp = np.zeros((cfg.channels, lay1.input_row_bytes), np.uint8)
     inp[:, :window.shape[1]] = window
     mid = np.zeros(lay1.output_bytes // 4, np.float32)
-    dd.subbandDedispersionStepOne(obs, stream.zapped, inp.reshape(-1), mid, stream.shifts,
-                                  cfg.padding, cfg.bits)
+    oracle.step_one(obs.c, stream.zapped, inp.reshape(-1), mid, stream.shifts, cfg.padding,
+                    cfg.bits)
     lay2 = dd.layout(obs, dd.DD_STEP_TWO, 32, cfg.padding)
     out = np.zeros(lay2.output_bytes // 4, np.float32)
     mapping = np.zeros(lay2.mapping_row_elems, np.uint32)
-    dd.subbandDedispersionStepTwo(obs, mapping, mid, out, stream.shifts2, cfg.padding)
+    oracle.step_two(obs.c, mapping, mid, out, stream.shifts2, cfg.padding)
     return out.reshape(-1, lay2.output_row_elems)[:, :S]
 
 
@@ -88,7 +90,7 @@ def serving_tail_step_two(stream):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("double_buffer", [False, True])
-def test_served_batches_equal_plain_path(gpu, double_buffer):
+def test_served_batches_equal_oracle(gpu, oracle, double_buffer):
     pytest.importorskip("torch")
     server = serving.Server(budget_bytes=150 * 10**9)
     beams = [dataclasses.replace(c, double_buffer=double_buffer) for c in small_beams()]
@@ -119,7 +121,7 @@ def test_served_batches_equal_plain_path(gpu, double_buffer):
         for k in range(nb):
             cur = inputs[(b, k)]
             window = np.concatenate([prev, cur], axis=1)
-            want = plain_reference(stream, window)
+            want = plain_reference(stream, window, oracle)
             got = outputs[(b, k)]
             assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (cfg.name, k)
             prev = window[:, window.shape[1] - tail_b:] if tail_b else prev
@@ -211,7 +213,7 @@ def test_time_major_double_buffered_stream(gpu):
 
 
 @pytest.mark.gpu
-def test_late_and_dropped_batches(gpu):
+def test_late_and_dropped_batches(gpu, oracle):
     """Faults injected on the host: beam 0's batch 1 arrives 0.12 s late (its
     deadline is 0.05 s after its nominal arrival), beam 1's batch 2 never
     arrives.  The late batch and the batch queued behind it miss their
@@ -250,7 +252,7 @@ def test_late_and_dropped_batches(gpu):
             cur = inputs.get((b, k), np.zeros((cfg.channels, cfg.samples), np.uint8))
             window = np.concatenate([prev, cur], axis=1)
             if (b, k) in outputs:
-                want = plain_reference(stream, window)
+                want = plain_reference(stream, window, oracle)
                 assert np.array_equal(outputs[(b, k)].view(np.uint32),
                                       want.view(np.uint32)), (cfg.name, k)
             prev = window[:, window.shape[1] - stream.tail:] if stream.tail else prev
@@ -258,7 +260,7 @@ def test_late_and_dropped_batches(gpu):
 
 
 @pytest.mark.gpu
-def test_file_source_serves_files(gpu, tmp_path):
+def test_file_source_serves_files(gpu, oracle, tmp_path):
     """Beams served straight from files (serving.FileSource): a SIGPROC
     filterbank with descending frequencies and a PSRDADA file with ascending
     ones, three batches each plus a partial fourth, read into the streams'
@@ -297,7 +299,7 @@ def test_file_source_serves_files(gpu, tmp_path):
         prev = np.zeros((C, stream.tail), np.uint8)
         for k in range(nb):
             window = np.concatenate([prev, padded[:, k * S:(k + 1) * S]], axis=1)
-            want = plain_reference(stream, window)
+            want = plain_reference(stream, window, oracle)
             assert np.array_equal(outputs[(b, k)].view(np.uint32), want.view(np.uint32)), (b, k)
             prev = window[:, window.shape[1] - stream.tail:]
     server.close()
